@@ -1,0 +1,453 @@
+#!/usr/bin/env python3
+"""Benchmark of the C2C FFT execute path on one GB300 (or N replicas).
+
+Default workload: 1D complex FP64 C2C, N = 2^24, forward + inverse (the
+single-transform case of the benchmark configuration "1D complex FP64 C2C
+forward+inverse: single N=2^24 and batched 256x2^16").  One step = one
+forward and one inverse transform of the device-resident array.
+
+  value     GFLOP/s (5 N log2 N per direction), whole job, device-resident
+            data (inputs in HBM when the timed region starts)
+  e2e       the same metric through the C interface with host buffers:
+            every step uploads the input from pinned memory (tope1DUpload)
+            and runs tope1DExec FORWARD and INVERSE, each of which reads the
+            result back into the host buffer (the reference's Exec contract)
+  roofline  the dominant kernel (the pass kernel): algorithmic bytes per
+            launch (2 * 16 B * points: one read and one write of the array)
+            over its average launch time, from CUDA events around every
+            launch inside the timed region, against the measured HBM copy
+            bandwidth
+  cpu_baseline  the reference's own kernels (oracle/_ref) or, where they
+            were not built, the oracle's restatement, on this host's cores,
+            on a bounded sample of the same workload
+
+--impl reference times only that CPU implementation (rank 0).
+Multi-GPU (torchrun): independent replicas, one per GPU, no collective on
+the data path; value = units of all ranks / max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+WORKLOADS = {
+    "1d_2p24": {"dims": (1 << 24, 1, 1), "batch": 1,
+                "desc": "1D C2C FP64, N=2^24, forward+inverse, uniform[-1,1) re/im"},
+    "1d_256x2p16": {"dims": (1 << 16, 1, 1), "batch": 256,
+                    "desc": "1D C2C FP64, batched 256 x 2^16, forward+inverse, uniform[-1,1) re/im"},
+    "2d_4096": {"dims": (4096, 4096, 1), "batch": 1,
+                "desc": "2D C2C FP64 4096x4096, forward+inverse, N(0,1) re/im"},
+    "3d_256": {"dims": (256, 256, 256), "batch": 1,
+               "desc": "3D C2C FP64 256^3, forward+inverse, N(0,1) re/im"},
+    "1d_4096": {"dims": (4096, 1, 1), "batch": 1,
+                "desc": "1D C2C FP64, N=4096, batch 1, forward+inverse, uniform[-1,1) re/im"},
+}
+METRIC = "C2C GFLOP/s & HBM GB/s vs roofline, FP64 plain vs split-precision at stated rel-L2"
+SEED0 = 0x70E0F0F7
+L2_BYTES = 129 * 10 ** 6
+FALLBACK_HBM_GBS = 6800.0
+# measured on a GB300 of this machine: DFMA 0.50 Tinstr/s (1.0 TFLOP/s)
+FP64_PIPE_TFLOPS = 1.0
+
+
+# ------------------------------------------------------------------ inputs
+def splitmix_uniform(n_complex: int, seed: int) -> np.ndarray:
+    """uniform[-1,1): value e = 2*u(seed, e) - 1, u from SplitMix64 >> 11."""
+    out = np.empty(2 * n_complex)
+    chunk = 1 << 22
+    with np.errstate(over="ignore"):
+        for s in range(0, 2 * n_complex, chunk):
+            idx = np.arange(s, min(s + chunk, 2 * n_complex), dtype=np.uint64)
+            z = np.uint64(seed) + (idx + np.uint64(1)) * np.uint64(0x9E3779B97F4A7C15)
+            z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+            z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+            z = z ^ (z >> np.uint64(31))
+            out[s:s + len(idx)] = 2.0 * ((z >> np.uint64(11)).astype(np.float64) * 2.0 ** -53) - 1.0
+    return out
+
+
+def splitmix_normal(n_complex: int, seed: int) -> np.ndarray:
+    u = splitmix_uniform(n_complex, seed)  # in [-1, 1)
+    u1 = (u[0::2] + 1.0) / 2.0
+    u2 = (u[1::2] + 1.0) / 2.0
+    r = np.sqrt(-2.0 * np.log1p(-u1))
+    out = np.empty(2 * n_complex)
+    out[0::2] = r * np.cos(2 * np.pi * u2)
+    out[1::2] = r * np.sin(2 * np.pi * u2)
+    return out
+
+
+def make_input(wl: dict) -> np.ndarray:
+    nx, ny, nz = wl["dims"]
+    n = nx * ny * nz * wl["batch"]
+    if ny * nz > 1:
+        return splitmix_normal(n, SEED0 + 3)
+    return splitmix_uniform(n, SEED0 + 2)
+
+
+def flops_per_step(wl: dict) -> float:
+    nx, ny, nz = wl["dims"]
+    n = nx * ny * nz
+    return 2 * 5.0 * n * np.log2(n) * wl["batch"]
+
+
+def p_min(n: int, fp32: bool = False) -> int:
+    return int(np.ceil(np.log2(n) / (14 if fp32 else 13)))
+
+
+# ------------------------------------------------------------------ helpers
+def measured_peaks() -> tuple[float, str]:
+    p = ROOT / "MEASURED_PEAKS.json"
+    try:
+        return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def ncu_traffic(workload: str, arith: str):
+    """Per-launch DRAM bytes of the dominant kernel from the committed ncu
+    summary for this workload (profiles/*.txt line 'traffic_bytes_per_launch:')."""
+    for p in sorted((ROOT / "profiles").glob(f"pass_kernel_{arith}_{workload}*.txt")):
+        for line in p.read_text().splitlines():
+            if line.startswith("traffic_bytes_per_launch:"):
+                try:
+                    return int(float(line.split(":", 1)[1].split()[0]))
+                except ValueError:
+                    return None
+    return None
+
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100", "-i", str(self.device)],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            time.sleep(0.6)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except Exception:
+            self.proc.kill()
+            out = ""
+        sm, smax, reasons, power = [], [], set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+                power.append(float(parts[3]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "power_w_max": max(power) if power else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def dist_init(ws: int, use_cuda: bool):
+    if ws <= 1:
+        return None
+    import torch.distributed as dist
+    if not dist.is_initialized():
+        dist.init_process_group("nccl" if use_cuda else "gloo")
+    return dist
+
+
+def max_over_ranks(dist, value: float, device=None) -> float:
+    """Max of a float over all ranks (identity without a process group)."""
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def aggregate(dist, local_ms_per_step: float, units_per_rank: float, device=None):
+    """Whole-job rate: all ranks' units over the slowest rank's time."""
+    ws = dist.get_world_size() if dist is not None else 1
+    ms = max_over_ranks(dist, local_ms_per_step, device)
+    return ms, units_per_rank * ws / (ms * 1e-3)
+
+
+# ------------------------------------------------------------------ CPU leg
+def cpu_reference_rate(wl: dict, budget_s: float = 30.0, steps: int = 1, warmup: int = 0):
+    """Time the reference's kernels (oracle/_ref) or the oracle's restatement
+    on the host cores; returns (GFLOP/s, dict).  The sample shrinks (1D: a
+    shorter length, others: fewer steps) when a full step would not fit."""
+    import oracle
+    kind = "reference" if oracle.REF_SO.exists() else "port"
+    emu = oracle.RefEmu() if kind == "reference" else oracle.Oracle()
+    cores = os.cpu_count() or 1
+    emu.set_threads(cores)
+    nx, ny, nz = wl["dims"]
+    batch = wl["batch"]
+    x = make_input(wl)
+
+    def one(xs, dims, b):
+        t0 = time.perf_counter()
+        if b == 1:
+            y = emu.exec(xs, *dims, 1)
+            emu.exec(y, *dims, 0)
+        else:  # the reference has no batched 1D: rows one by one
+            n = dims[0]
+            for i in range(b):
+                row = xs[2 * n * i: 2 * n * (i + 1)]
+                y = emu.exec(row, n, 1, 1, 1)
+                emu.exec(y, n, 1, 1, 0)
+        return time.perf_counter() - t0
+
+    sample_dims, sample_batch, xs = (nx, ny, nz), batch, x
+    if batch > 1:  # time a bounded number of rows
+        sample_batch = min(batch, 16)
+        xs = x[: 2 * nx * sample_batch]
+    for _ in range(warmup):
+        one(xs, sample_dims, sample_batch)
+    times = []
+    t_start = time.perf_counter()
+    for _ in range(max(1, steps)):
+        times.append(one(xs, sample_dims, sample_batch))
+        if time.perf_counter() - t_start > budget_s:
+            break
+    t = statistics.median(times)
+    n_s = sample_dims[0] * sample_dims[1] * sample_dims[2]
+    flops = 2 * 5.0 * n_s * np.log2(n_s) * sample_batch
+    gflops = flops / t / 1e9
+    sample = (f"{'x'.join(map(str, sample_dims))} x batch {sample_batch}, forward+inverse, "
+              f"{len(times)} timed step(s), median {t:.3f} s, {cores} threads")
+    return gflops, {"value": round(gflops, 4), "unit": "GFLOP/s", "cores": cores, "kind": kind,
+                    "sample": sample, "ms_per_step": t * 1e3}
+
+
+# ------------------------------------------------------------------ GPU leg
+def run_gpu(args, wl: dict) -> dict:
+    import torch
+    import __graft_entry__ as g
+    T = g.load_package()
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    os.environ["TOPEFFT_DEVICE"] = str(local)
+    dist = dist_init(ws, True)
+    nx, ny, nz = wl["dims"]
+    batch = wl["batch"]
+    n = nx * ny * nz
+    total = n * batch
+    x = make_input(wl)
+
+    f = T.TopeFFT()
+    T.topeFFTInit(f)
+    T.check(f)
+    T.topeSetArith(f, T.TOPE_ARITH_DF64 if args.arith == "df64" else T.TOPE_ARITH_FP64)
+    d = x.copy()
+    if ny * nz == 1:
+        t = T.TopePlan1D()
+        if batch == 1:
+            T.tope1DPlanInit(f, t, nx, T.C2C, d)
+        else:
+            T.tope1DBatchPlanInit(f, t, nx, batch, T.C2C, d)
+    elif nz == 1:
+        t = T.TopePlan2D()
+        T.tope2DPlanInit(f, t, nx, ny, T.C2C, d)
+    else:
+        t = T.TopePlan3D()
+        T.tope3DPlanInit(f, t, nx, ny, nz, T.C2C, d)
+    T.check(f)
+    stream = torch.cuda.ExternalStream(f.command_queue)
+
+    def step():
+        T.execDevice(f, t, T.FORWARD)
+        T.execDevice(f, t, T.INVERSE)
+
+    for _ in range(args.warmup):
+        step()
+    T.topeSync(f)
+    T.topeSetPassTiming(f, 1)
+    T.lib.topeResetPassTimes(ctypes.byref(f), t.impl)
+    sampler = ClockSampler(local)
+    sampler.start()
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    T.topeSync(f)
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    clocks = sampler.stop()
+    T.check(f)
+    ms_local = e0.elapsed_time(e1) / args.steps
+    passes = T.pass_times(f, t)
+    T.topeSetPassTiming(f, 0)
+    ms, value = aggregate(dist, ms_local, flops_per_step(wl), device=torch.device("cuda", local))
+    value_gflops = value / 1e9
+    launches = sum(p["launches"] for p in passes)
+
+    # accuracy after W+K round trips (forward then inverse each step)
+    back = np.empty_like(x)
+    T.download(f, t, back)
+    rt = float(np.sqrt(np.sum((back - x) ** 2) / np.sum(x * x)))
+
+    # dominant kernel: the pass with the largest total time
+    dom = max(passes, key=lambda p: p["ns"]) if passes else None
+    bytes_per_launch = 2 * 16 * total
+    peak, peak_kind = measured_peaks()
+    roof = None
+    if dom and dom["launches"]:
+        avg_ns = dom["ns"] / dom["launches"]
+        ach = bytes_per_launch / avg_ns  # bytes/ns == GB/s
+        roof = {"bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(ach / peak, 4), "peak_source": peak_kind,
+                "traffic": ncu_traffic(args.workload, args.arith),
+                "kernel": f"pass_kernel L=2^{dom['log_l']} B={dom['b_tile']} "
+                          f"({dom['ctas']} CTAs x {dom['threads']} threads)",
+                "launch_us": round(avg_ns / 1e3, 2),
+                "bytes_per_launch": bytes_per_launch,
+                "fp64_pipe_tflops_measured": FP64_PIPE_TFLOPS}
+
+    # e2e through the C interface with pinned host buffers
+    nbytes = x.nbytes
+    hp = T.lib.topeHostAlloc(nbytes)
+    host = np.ctypeslib.as_array((ctypes.c_double * (2 * total)).from_address(hp))
+    host[:] = x
+    exec_fn = {T.TopePlan1D: T.tope1DExec, T.TopePlan2D: T.tope2DExec,
+               T.TopePlan3D: T.tope3DExec}[type(t)]
+
+    def e2e_step():
+        T.upload(f, t, hp)
+        exec_fn(f, t, hp, T.FORWARD)
+        exec_fn(f, t, hp, T.INVERSE)
+
+    e2e_steps = max(3, min(args.steps, 20))
+    e2e_step()
+    if dist is not None:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_step()
+    t1 = time.perf_counter()
+    T.check(f)
+    e2e_ms, e2e_val = aggregate(dist, (t1 - t0) * 1e3 / e2e_steps, flops_per_step(wl),
+                                device=torch.device("cuda", local))
+    T.lib.topeHostFree(hp)
+
+    if ny * nz == 1:
+        T.tope1DDestroy(f, t)
+    elif nz == 1:
+        T.tope2DDestroy(f, t)
+    else:
+        T.tope3DDestroy(f, t)
+
+    res = {
+        "metric": METRIC, "value": round(value_gflops, 3), "unit": "GFLOP/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (SplitMix64-seeded)",
+        "config": {"workload": args.workload, "description": wl["desc"],
+                   "arith": "double-float (FP32 pairs) on FP64 storage" if args.arith == "df64"
+                   else "native FP64",
+                   "points": total, "l2": f"inputs larger than L2 ({total * 16 >> 20} MiB array vs "
+                                          f"129 MB L2)" if total * 16 > L2_BYTES else
+                   "array fits in L2 (latency-bound size)",
+                   "parallelism": f"replicas x{ws}"},
+        "hbm_gbs_effective": round(p_min(n) * 2 * 16 * total * 2 / (ms * 1e-3) / 1e9, 1),
+        "rel_l2_roundtrip": rt,
+        "roofline": roof,
+        "passes": passes,
+        "e2e": {"value": round(e2e_val / 1e9, 3), "unit": "GFLOP/s",
+                "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": 2 * nbytes,
+                "ms_per_step": round(e2e_ms, 3)},
+        "gpu_launches": launches,
+        "clocks": clocks,
+    }
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        _, cpu = cpu_reference_rate(wl, budget_s=30.0, steps=1)
+        res["cpu_baseline"] = cpu
+    if dist is not None:
+        dist.destroy_process_group()
+    return res if rank == 0 else None
+
+
+def run_reference(args, wl: dict):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return None
+    gflops, cpu = cpu_reference_rate(wl, budget_s=150.0 / max(1, args.steps + args.warmup) * args.steps,
+                                     steps=args.steps, warmup=min(args.warmup, 1))
+    return {"impl": "reference", "metric": METRIC, "value": round(gflops, 4), "unit": "GFLOP/s",
+            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(cpu["ms_per_step"], 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (SplitMix64-seeded)",
+            "config": {"workload": args.workload, "description": wl["desc"],
+                       "parallelism": "host cores of rank 0"},
+            "cpu_baseline": cpu,
+            "e2e": {"value": round(gflops, 4), "unit": "GFLOP/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="1d_2p24")
+    ap.add_argument("--arith", choices=["fp64", "df64"], default="fp64")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args(argv)
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    wl = WORKLOADS[args.workload]
+    res = run_reference(args, wl) if args.impl == "reference" else run_gpu(args, wl)
+    if res is not None:
+        print(json.dumps(res), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,104 @@
+/*
+ * topefft_ext.h - extensions of the GB300 FFT library beyond the reference's
+ * surface.  None of these has a counterpart in the reference's topefft.h;
+ * each is named for what it adds.  Include after topefft.h.
+ */
+#ifndef TOPEFFT_EXT_H
+#define TOPEFFT_EXT_H
+
+#include "topefft.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (the reference asserts instead, topefft.h:6) ---------- */
+enum topeStatus {
+    TOPE_SUCCESS = 0,
+    TOPE_ERR_INVALID_SIZE = 1,   /* length not supported (e.g. 2D/3D non power of two) */
+    TOPE_ERR_INVALID_ARG = 2,    /* NULL pointer, bad direction or type */
+    TOPE_ERR_ALLOC = 3,          /* device or host allocation failed */
+    TOPE_ERR_CUDA = 4,           /* a CUDA call failed; see topeLastCudaError() */
+    TOPE_ERR_NOT_INITIALIZED = 5,/* framework not initialised */
+    TOPE_ERR_DESTROYED = 6,      /* plan already destroyed (double destroy, use after destroy) */
+    TOPE_ERR_UNSUPPORTED = 7,    /* valid request this build cannot run (e.g. R2C) */
+    TOPE_ERR_TIMEOUT = 8         /* a bounded device-side wait expired */
+};
+
+/* Status of the most recent failing call on this thread; reading it resets
+ * it to TOPE_SUCCESS (the same contract as cudaGetLastError). */
+int topeGetLastError(void);
+/* Same, without resetting. */
+int topePeekLastError(void);
+const char *topeErrorString(int status);
+/* CUDA error code behind the last TOPE_ERR_CUDA on this thread. */
+int topeLastCudaError(void);
+
+/* ---- arithmetic option --------------------------------------------------- */
+/* Storage and I/O are FP64 for both.  TOPE_ARITH_FP64 computes butterflies
+ * with double-precision instructions.  TOPE_ARITH_DF64 computes them as
+ * FP32 (hi, lo) pairs with error-free transformations on the FP32 pipe
+ * (about 2^-44 relative per operation), which on GB300 runs much faster
+ * than its FP64 pipe; accuracy is gated by the same rel-L2 <= 1e-13*log2(N)
+ * bound.  Applies to plans created after the call. */
+enum topeArith { TOPE_ARITH_FP64 = 0, TOPE_ARITH_DF64 = 1 };
+void topeSetArith(struct topeFFT *f, int arith);
+
+/* ---- framework lifetime -------------------------------------------------- */
+/* Releases the framework's stream.  The reference releases its queue and
+ * context inside every Destroy (fft1d.c:385-392); here plans are counted
+ * and the stream is released when the last plan goes, or by this call. */
+void topeFFTDestroy(struct topeFFT *f);
+
+/* ---- device-resident execution (no host copies) ------------------------- */
+/* Transform the plan's device array in place without the read-back of
+ * tope*Exec.  Asynchronous on f->command_queue; kernel time is added to
+ * totalKernel at the next synchronising call. */
+void tope1DExecDevice(struct topeFFT *f, struct topePlan1D *t, int dir);
+void tope2DExecDevice(struct topeFFT *f, struct topePlan2D *t, int dir);
+void tope3DExecDevice(struct topeFFT *f, struct topePlan3D *t, int dir);
+/* Copy host data into / out of the plan's device array (synchronous). */
+void tope1DUpload(struct topeFFT *f, struct topePlan1D *t, const double *d);
+void tope1DDownload(struct topeFFT *f, struct topePlan1D *t, double *d);
+void tope2DUpload(struct topeFFT *f, struct topePlan2D *t, const double *d);
+void tope2DDownload(struct topeFFT *f, struct topePlan2D *t, double *d);
+void tope3DUpload(struct topeFFT *f, struct topePlan3D *t, const double *d);
+void tope3DDownload(struct topeFFT *f, struct topePlan3D *t, double *d);
+/* Wait for all work queued on the framework's stream. */
+void topeSync(struct topeFFT *f);
+
+/* ---- batched 1D ----------------------------------------------------------- */
+/* batch contiguous transforms of length x (row b at d + 2*b*x).  The plan is
+ * a topePlan1D; tope1DExec / tope1DExecDevice / Upload / Download / Destroy
+ * apply to all rows.  dataSize = 16*x*batch. */
+void tope1DBatchPlanInit(struct topeFFT *f, struct topePlan1D *t, int x, int batch, int type,
+                         double *d);
+
+/* ---- tables and permutation (plan internals, exposed for inspection) ---- */
+/* Copy a device buffer to host memory (synchronous). */
+void topeCopyToHost(struct topeFFT *f, void *dst, const void *device_src, size_t bytes);
+/* Apply the bit-reversal permutation of length 2^log2n in place along axis
+ * (0 = x, 1 = y, 2 = z) of the plan's device array: the reference's swap
+ * pass (kernels3D.cl:574-637), bit for bit. */
+void tope3DBitrevPermute(struct topeFFT *f, struct topePlan3D *t, int axis);
+/* Pinned host memory, for callers that want fast copies. */
+void *topeHostAlloc(size_t bytes);
+void topeHostFree(void *p);
+
+/* ---- per-launch kernel timing ------------------------------------------- */
+/* When enabled, every pass launch of plans of this framework is bracketed
+ * by a CUDA event pair on f->command_queue; durations are folded in at the
+ * next synchronising call.  impl is a plan's t->impl. */
+void topeSetPassTiming(struct topeFFT *f, int enable);
+/* Writes up to max per-pass totals (ns) and launch counts; returns the
+ * plan's number of passes. */
+int topePassTimes(struct topeFFT *f, void *impl, uint64_t *ns, uint64_t *launches, int max);
+void topeResetPassTimes(struct topeFFT *f, void *impl);
+/* Geometry of pass i of a plan: {log2 L, lines per CTA, CTAs, threads per
+ * CTA, out-of-place, four-step twiddle}; returns 0, or -1 if i is out of range. */
+int topePassInfo(struct topeFFT *f, void *impl, int i, int64_t info[6]);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,265 @@
+/*
+ * Runtime wrappers, plan-time table kernels and the small auxiliary kernels
+ * of the C2C path.  Every entry point is extern "C" with plain types; the C
+ * host library (topefft.c) is the only caller.
+ */
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "fft_arith.cuh"
+#include "tfft_abi.h"
+
+/* ------------------------------------------------------------------------ */
+/* runtime                                                                  */
+/* ------------------------------------------------------------------------ */
+extern "C" {
+
+int tfft_set_device(int dev) { return (int)cudaSetDevice(dev); }
+int tfft_get_device(int *dev) { return (int)cudaGetDevice(dev); }
+int tfft_device_count(int *n) { return (int)cudaGetDeviceCount(n); }
+int tfft_malloc(void **p, size_t bytes) { return (int)cudaMalloc(p, bytes ? bytes : 16); }
+int tfft_free(void *p) { return p ? (int)cudaFree(p) : 0; }
+int tfft_host_alloc(void **p, size_t bytes) { return (int)cudaMallocHost(p, bytes ? bytes : 16); }
+int tfft_host_free(void *p) { return p ? (int)cudaFreeHost(p) : 0; }
+int tfft_memset_async(void *p, int v, size_t bytes, void *s)
+{
+    return (int)cudaMemsetAsync(p, v, bytes, (cudaStream_t)s);
+}
+int tfft_h2d(void *dst, const void *src, size_t bytes, void *s)
+{
+    return (int)cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, (cudaStream_t)s);
+}
+int tfft_d2h(void *dst, const void *src, size_t bytes, void *s)
+{
+    return (int)cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, (cudaStream_t)s);
+}
+int tfft_d2d(void *dst, const void *src, size_t bytes, void *s)
+{
+    return (int)cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, (cudaStream_t)s);
+}
+int tfft_stream_create(void **s)
+{
+    cudaStream_t st;
+    cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+    *s = (void *)st;
+    return (int)e;
+}
+int tfft_stream_destroy(void *s) { return s ? (int)cudaStreamDestroy((cudaStream_t)s) : 0; }
+int tfft_stream_sync(void *s) { return (int)cudaStreamSynchronize((cudaStream_t)s); }
+int tfft_event_create(void **e)
+{
+    cudaEvent_t ev;
+    cudaError_t r = cudaEventCreate(&ev);
+    *e = (void *)ev;
+    return (int)r;
+}
+int tfft_event_destroy(void *e) { return e ? (int)cudaEventDestroy((cudaEvent_t)e) : 0; }
+int tfft_event_record(void *e, void *s) { return (int)cudaEventRecord((cudaEvent_t)e, (cudaStream_t)s); }
+int tfft_event_elapsed_ns(void *a, void *b, uint64_t *ns)
+{
+    float ms = 0.f;
+    cudaError_t r = cudaEventElapsedTime(&ms, (cudaEvent_t)a, (cudaEvent_t)b);
+    *ns = r == cudaSuccess ? (uint64_t)((double)ms * 1.0e6 + 0.5) : 0;
+    return (int)r;
+}
+int tfft_last_launch_error(void) { return (int)cudaGetLastError(); }
+const char *tfft_error_string(int code) { return cudaGetErrorString((cudaError_t)code); }
+
+} /* extern "C" */
+
+/* ------------------------------------------------------------------------ */
+/* tables                                                                   */
+/* ------------------------------------------------------------------------ */
+namespace {
+
+/* exp(-2 pi i m / n) for n = 2^log_n: the argument 2m/n is exact, so the
+ * only rounding is sincospi's own. */
+__device__ __forceinline__ double2 w_pow2(int64_t m, int log_n)
+{
+    double s, c;
+    sincospi(ldexp((double)m, 1 - log_n), &s, &c);
+    return make_double2(c, -s);
+}
+
+__device__ __forceinline__ void put_tw(void *tab, int64_t i, double2 w, int arith)
+{
+    if (arith == TFFT_ARITH_F64) {
+        reinterpret_cast<double2 *>(tab)[i] = w;
+    } else {
+        float rh = __double2float_rn(w.x), ih = __double2float_rn(w.y);
+        float rl = __double2float_rn(w.x - (double)rh), il = __double2float_rn(w.y - (double)ih);
+        reinterpret_cast<float4 *>(tab)[i] = make_float4(rh, rl, ih, il);
+    }
+}
+
+__global__ void k_twiddle(void *tw, int log_l, int arith)
+{
+    const int64_t L = int64_t(1) << log_l;
+    for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < L;
+         m += (int64_t)gridDim.x * blockDim.x)
+        put_tw(tw, m, w_pow2(m, log_l), arith);
+}
+
+__global__ void k_fourstep(void *hi, void *lo, int log_n, int shift, int arith)
+{
+    const int64_t nlo = int64_t(1) << shift, nhi = int64_t(1) << (log_n - shift);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nlo + nhi;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        if (i < nlo) put_tw(lo, i, w_pow2(i, log_n), arith);
+        else put_tw(hi, i - nlo, w_pow2((i - nlo) << shift, log_n), arith);
+    }
+}
+
+__global__ void k_bitrev(int *rev, int log2n)
+{
+    const int64_t n = int64_t(1) << log2n;
+    for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n;
+         g += (int64_t)gridDim.x * blockDim.x)
+        rev[g] = log2n ? (int)(__brev((unsigned)g) >> (32 - log2n)) : 0;
+}
+
+/* The reference's plan table, src/kernels1D.cl:7-13: entries k < n/4. */
+__global__ void k_quarter(double2 *tw, int n)
+{
+    int log_n = 0;
+    while ((1 << log_n) < n) log_n++;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n / 4; k += gridDim.x * blockDim.x)
+        tw[k] = w_pow2(k, log_n);
+}
+
+/* W_n^m for any n (DFT path): sincospi(2m/n) with the quotient rounded once */
+__global__ void k_dft_table(double2 *tw, int n)
+{
+    for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < n; m += gridDim.x * blockDim.x) {
+        double s, c;
+        sincospi(2.0 * (double)m / (double)n, &s, &c);
+        tw[m] = make_double2(c, -s);
+    }
+}
+
+/* out[k] = sum_j in[j] W_n^{jk}; twiddle index advanced modulo n exactly */
+__global__ void k_dft(const double2 *__restrict__ in, double2 *__restrict__ out,
+                      const double2 *__restrict__ tw, int n, int dir)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    double sr = 0.0, si = 0.0;
+    int m = 0;
+    for (int j = 0; j < n; j++) {
+        const double2 x = in[j];
+        double2 w = __ldg(tw + m);
+        if (!dir) w.y = -w.y;
+        sr = fma(x.x, w.x, fma(-x.y, w.y, sr));
+        si = fma(x.x, w.y, fma(x.y, w.x, si));
+        m += k;
+        if (m >= n) m -= n;
+    }
+    const double s = dir ? 1.0 : 1.0 / (double)n;
+    out[k] = make_double2(sr * s, si * s);
+}
+
+/* In-place bit-reversal permutation along an axis, the reference's swap
+ * (src/kernels3D.cl:574-637): element i of a line trades places with
+ * rev[i] when i < rev[i].  One thread per (line, i). */
+__global__ void k_bitrev_permute(double2 *d, const int *__restrict__ rev, int log2n, int64_t es,
+                                 int64_t n0, int64_t s0, int64_t n1, int64_t s1)
+{
+    const int64_t n = int64_t(1) << log2n;
+    const int64_t total = n * n0 * n1;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t g0 = t % n0, rest = t / n0;
+        const int64_t i = rest % n, g1 = rest / n;
+        const int64_t r = rev[i];
+        if (i < r) {
+            double2 *line = d + g0 * s0 + g1 * s1;
+            const double2 a = line[i * es], b = line[r * es];
+            line[i * es] = b;
+            line[r * es] = a;
+        }
+    }
+}
+
+__global__ void k_n2(double2 *d, int dir)
+{
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        const double2 a = d[0], b = d[1];
+        double2 x = make_double2(a.x + b.x, a.y + b.y), y = make_double2(a.x - b.x, a.y - b.y);
+        if (!dir) {
+            x.x *= 0.5; x.y *= 0.5;
+            y.x *= 0.5; y.y *= 0.5;
+        }
+        d[0] = x;
+        d[1] = y;
+    }
+}
+
+inline unsigned grid_for(int64_t n, int threads)
+{
+    int64_t g = (n + threads - 1) / threads;
+    if (g < 1) g = 1;
+    if (g > 152 * 32) g = 152 * 32;
+    return (unsigned)g;
+}
+
+} // namespace
+
+extern "C" {
+
+int tfft_twiddle_table(void *tw, int log_l, int arith, void *s)
+{
+    k_twiddle<<<grid_for(int64_t(1) << log_l, 256), 256, 0, (cudaStream_t)s>>>(tw, log_l, arith);
+    return (int)cudaGetLastError();
+}
+
+int tfft_fourstep_tables(void *hi, void *lo, int64_t n, int shift, int arith, void *s)
+{
+    int log_n = 0;
+    while ((int64_t(1) << log_n) < n) log_n++;
+    const int64_t cnt = (int64_t(1) << shift) + (n >> shift);
+    k_fourstep<<<grid_for(cnt, 256), 256, 0, (cudaStream_t)s>>>(hi, lo, log_n, shift, arith);
+    return (int)cudaGetLastError();
+}
+
+int tfft_bitrev_table(int *rev, int log2n, void *s)
+{
+    k_bitrev<<<grid_for(int64_t(1) << log2n, 256), 256, 0, (cudaStream_t)s>>>(rev, log2n);
+    return (int)cudaGetLastError();
+}
+
+int tfft_quarter_table(void *tw, int n, void *s)
+{
+    if (n < 4) return 0;
+    k_quarter<<<grid_for(n / 4, 256), 256, 0, (cudaStream_t)s>>>((double2 *)tw, n);
+    return (int)cudaGetLastError();
+}
+
+int tfft_dft_table(void *tw, int n, void *s)
+{
+    k_dft_table<<<grid_for(n, 256), 256, 0, (cudaStream_t)s>>>((double2 *)tw, n);
+    return (int)cudaGetLastError();
+}
+
+int tfft_launch_dft(const void *in, void *out, const void *tw, int n, int dir, void *s)
+{
+    k_dft<<<(n + 127) / 128, 128, 0, (cudaStream_t)s>>>((const double2 *)in, (double2 *)out,
+                                                       (const double2 *)tw, n, dir);
+    return (int)cudaGetLastError();
+}
+
+int tfft_launch_bitrev_permute(void *d, const int *rev, int log2n, int64_t es, int64_t n0,
+                               int64_t s0, int64_t n1, int64_t s1, void *s)
+{
+    const int64_t total = (int64_t(1) << log2n) * n0 * n1;
+    k_bitrev_permute<<<grid_for(total, 256), 256, 0, (cudaStream_t)s>>>((double2 *)d, rev, log2n,
+                                                                       es, n0, s0, n1, s1);
+    return (int)cudaGetLastError();
+}
+
+int tfft_launch_n2(void *d, int dir, void *s)
+{
+    k_n2<<<1, 32, 0, (cudaStream_t)s>>>((double2 *)d, dir);
+    return (int)cudaGetLastError();
+}
+
+} /* extern "C" */

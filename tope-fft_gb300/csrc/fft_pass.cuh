@@ -1,0 +1,283 @@
+/*
+ * The pass kernel: batched power-of-two FFTs of length L = 2^LOG_L <= 8192,
+ * one tile of B lines per CTA, entirely on chip.
+ *
+ * Algorithm (replaces the reference's swap pass plus one global-memory pass
+ * per radix stage, src/fft1d.c:41-114, src/kernels1D.cl:15-547):
+ *   - each thread owns E = min(16, L) points of one line, loaded with a
+ *     coalesced pattern: thread j holds elements j + q*L/E (q < E);
+ *   - Stockham autosort stages: an optional first stage of radix
+ *     2^(LOG_L mod 4) and then radix-16 stages, each a register butterfly
+ *     preceded by W_{Ns*R}^{r*k} twiddles from a per-L table (one rounding
+ *     per factor, sincospi in FP64); stages exchange through shared memory
+ *     laid out as (p + p/16) * B + b, which keeps 16-byte accesses free of
+ *     bank conflicts for every stage;
+ *   - the result comes out in natural order in the same registers, so no
+ *     bit-reversal permutation pass is needed;
+ *   - fused on the way out: optional four-step twiddle, conjugation and the
+ *     exact 1/N scaling of the inverse (src/kernels1D.cl:499-503).
+ * Thread (j, b) maps to threadIdx.x = j*B + b, so the B lines of a tile are
+ * the fastest-varying thread index: when lines are adjacent in memory
+ * (strided axes of 2D/3D arrays and the four-step passes) each group of B
+ * threads reads or writes B*16 contiguous bytes.
+ */
+#pragma once
+#include "fft_arith.cuh"
+#include "tfft_abi.h"
+
+namespace tfft {
+
+template <class A>
+__device__ __forceinline__ void dft2(typename A::C &a0, typename A::C &a1)
+{
+    typename A::C t = A::sub(a0, a1);
+    a0 = A::add(a0, a1);
+    a1 = t;
+}
+
+template <class A>
+__device__ __forceinline__ void dft4(typename A::C &a0, typename A::C &a1,
+                                     typename A::C &a2, typename A::C &a3)
+{
+    using C = typename A::C;
+    C t0 = A::add(a0, a2), t1 = A::sub(a0, a2);
+    C t2 = A::add(a1, a3), t3 = A::mul_mi(A::sub(a1, a3));
+    a0 = A::add(t0, t2);
+    a2 = A::sub(t0, t2);
+    a1 = A::add(t1, t3);
+    a3 = A::sub(t1, t3);
+}
+
+/* 8 = 4 (inner, stride-2 inputs) x 2 (outer) */
+template <class A>
+__device__ __forceinline__ void dft8(typename A::C *c)
+{
+    using C = typename A::C;
+    dft4<A>(c[0], c[2], c[4], c[6]);
+    dft4<A>(c[1], c[3], c[5], c[7]);
+    c[3] = A::mul_w8(c[3]);
+    c[5] = A::mul_mi(c[5]);
+    c[7] = A::mul_w8_3(c[7]);
+    C y[8];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        y[k] = A::add(c[2 * k], c[2 * k + 1]);
+        y[k + 4] = A::sub(c[2 * k], c[2 * k + 1]);
+    }
+#pragma unroll
+    for (int k = 0; k < 8; k++) c[k] = y[k];
+}
+
+/* 16 = 4 (inner, stride-4 inputs) x 4 (outer), internal twiddles W16^{n2 k1} */
+template <class A>
+__device__ __forceinline__ void dft16(typename A::C *c)
+{
+    using C = typename A::C;
+#pragma unroll
+    for (int n2 = 0; n2 < 4; n2++) dft4<A>(c[n2], c[n2 + 4], c[n2 + 8], c[n2 + 12]);
+    /* Y[n2][k1] lives in c[n2 + 4*k1] */
+    c[5] = A::template mul_w16<1>(c[5]);
+    c[9] = A::mul_w8(c[9]);
+    c[13] = A::template mul_w16<3>(c[13]);
+    c[6] = A::mul_w8(c[6]);
+    c[10] = A::mul_mi(c[10]);
+    c[14] = A::mul_w8_3(c[14]);
+    c[7] = A::template mul_w16<3>(c[7]);
+    c[11] = A::mul_w8_3(c[11]);
+    c[15] = A::neg(A::template mul_w16<1>(c[15]));
+#pragma unroll
+    for (int k1 = 0; k1 < 4; k1++) dft4<A>(c[4 * k1], c[4 * k1 + 1], c[4 * k1 + 2], c[4 * k1 + 3]);
+    /* X[k1 + 4*k2] is in c[4*k1 + k2]: transpose the 4x4 register block */
+    C y[16];
+#pragma unroll
+    for (int k1 = 0; k1 < 4; k1++)
+#pragma unroll
+        for (int k2 = 0; k2 < 4; k2++) y[k1 + 4 * k2] = c[4 * k1 + k2];
+#pragma unroll
+    for (int k = 0; k < 16; k++) c[k] = y[k];
+}
+
+template <class A, int R>
+__device__ __forceinline__ void dft(typename A::C *c)
+{
+    if constexpr (R == 2) dft2<A>(c[0], c[1]);
+    else if constexpr (R == 4) dft4<A>(c[0], c[1], c[2], c[3]);
+    else if constexpr (R == 8) dft8<A>(c);
+    else if constexpr (R == 16) dft16<A>(c);
+}
+
+/* padded shared-memory index of element p of tile line b */
+template <int B>
+__device__ __forceinline__ int sidx(int p, int b) { return (p + (p >> 4)) * B + b; }
+
+template <int LOG_L>
+struct Shape {
+    static constexpr int L = 1 << LOG_L;
+    static constexpr int E = L < 16 ? L : 16;      /* points per thread */
+    static constexpr int TPL = L / E;              /* threads per line */
+    static constexpr int LR0 = LOG_L <= 4 ? LOG_L : (LOG_L % 4);
+    static constexpr int R0 = 1 << LR0;            /* first-stage radix */
+    static constexpr int NSTAGE = LOG_L <= 4 ? 1 : (LR0 ? 1 : 0) + LOG_L / 4;
+};
+
+template <class A, int LOG_L, int B>
+constexpr size_t pass_smem_bytes()
+{
+    return Shape<LOG_L>::TPL > 1
+               ? (size_t)((1 << LOG_L) + ((1 << LOG_L) >> 4)) * B * sizeof(typename A::S)
+               : 0;
+}
+
+/*
+ * One Stockham stage of radix R after Ns points have been combined.
+ * Reads its inputs from shared memory unless it is the first stage (the
+ * registers then already hold the loaded points); writes to shared memory
+ * unless it is the last stage (the registers then hold natural-order output).
+ */
+template <class A, int LOG_L, int B, int R, int NS, bool FROM_SMEM, bool TO_SMEM>
+__device__ __forceinline__ void stage(typename A::C *a, typename A::S *sm, int j, int b,
+                                      const void *tw)
+{
+    using C = typename A::C;
+    using SH = Shape<LOG_L>;
+    constexpr int L = SH::L, E = SH::E, TPL = SH::TPL;
+    if constexpr (FROM_SMEM) {
+#pragma unroll
+        for (int q = 0; q < E; q++) a[q] = A::from_smem(sm[sidx<B>(j + q * TPL, b)]);
+    }
+#pragma unroll
+    for (int u = 0; u < E / R; u++) {
+        C c[R];
+#pragma unroll
+        for (int r = 0; r < R; r++) c[r] = a[u + r * (E / R)];
+        if constexpr (NS > 1) {
+            const int k = (j + u * TPL) & (NS - 1);
+#pragma unroll
+            for (int r = 1; r < R; r++)
+                c[r] = A::mul_tw(c[r], A::load_tw(tw, (int64_t)(r * k) * (L / (NS * R))));
+        }
+        dft<A, R>(c);
+#pragma unroll
+        for (int r = 0; r < R; r++) a[u + r * (E / R)] = c[r];
+    }
+    if constexpr (TO_SMEM) {
+        if constexpr (FROM_SMEM) __syncthreads();
+#pragma unroll
+        for (int u = 0; u < E / R; u++) {
+            const int jj = j + u * TPL;
+            const int k = jj & (NS - 1);
+            const int o = (jj / NS) * NS * R + k;
+#pragma unroll
+            for (int r = 0; r < R; r++) sm[sidx<B>(o + r * NS, b)] = A::to_smem(a[u + r * (E / R)]);
+        }
+        __syncthreads();
+    }
+}
+
+/* stages after the first: radix 16, Ns = R0 * 16^s */
+template <class A, int LOG_L, int B, int S>
+__device__ __forceinline__ void stages16(typename A::C *a, typename A::S *sm, int j, int b,
+                                         const void *tw)
+{
+    using SH = Shape<LOG_L>;
+    if constexpr (S < SH::NSTAGE) {
+        constexpr int first_log = SH::LR0 ? SH::LR0 : 4;
+        constexpr int NS = 1 << (first_log + 4 * (S - 1));
+        constexpr bool last = (S == SH::NSTAGE - 1);
+        stage<A, LOG_L, B, 16, NS, true, !last>(a, sm, j, b, tw);
+        stages16<A, LOG_L, B, S + 1>(a, sm, j, b, tw);
+    }
+}
+
+template <class A, int LOG_L, int B>
+__device__ __forceinline__ void fft_line_regs(typename A::C *a, typename A::S *sm, int j, int b,
+                                              const void *tw)
+{
+    using SH = Shape<LOG_L>;
+    if constexpr (LOG_L == 0) {
+        return;
+    } else if constexpr (SH::NSTAGE == 1) {
+        stage<A, LOG_L, B, SH::R0, 1, false, false>(a, sm, j, b, tw);
+    } else {
+        constexpr int R_first = SH::LR0 ? SH::R0 : 16;
+        stage<A, LOG_L, B, R_first, 1, false, true>(a, sm, j, b, tw);
+        stages16<A, LOG_L, B, 1>(a, sm, j, b, tw);
+    }
+}
+
+template <class A, int LOG_L, int B>
+__global__ void __launch_bounds__(Shape<LOG_L>::TPL * B)
+    pass_kernel(const tfft_pass p)
+{
+    using C = typename A::C;
+    using SH = Shape<LOG_L>;
+    constexpr int E = SH::E, TPL = SH::TPL;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    typename A::S *sm = reinterpret_cast<typename A::S *>(smem_raw);
+
+    const int tid = threadIdx.x;
+    const int b = tid % B, j = tid / B;
+    const int64_t tiles0 = p.n[0] / B;
+    const int64_t blk = blockIdx.x;
+    const int64_t g0 = (blk % tiles0) * B + b;
+    const int64_t rest = blk / tiles0;
+    const int64_t g1 = rest % p.n[1], g2 = rest / p.n[1];
+
+    const double2 *in = reinterpret_cast<const double2 *>(p.in) + g0 * p.is[0] + g1 * p.is[1] +
+                        g2 * p.is[2];
+    C a[E];
+#pragma unroll
+    for (int q = 0; q < E; q++) {
+        C v = A::load(__ldcs(in + (int64_t)(j + q * TPL) * p.ies));
+        a[q] = p.conj_in ? A::conj(v) : v;
+    }
+
+    fft_line_regs<A, LOG_L, B>(a, sm, j, b, p.tw);
+
+    if (p.post_tw) {
+        const int64_t t = p.tw_level == 0 ? g0 : g1;
+        const int64_t mask = (int64_t(1) << p.tw_shift) - 1;
+#pragma unroll
+        for (int q = 0; q < E; q++) {
+            const int64_t m = (t * (int64_t)(j + q * TPL)) & (p.tw_n - 1);
+            typename A::TW w = A::tw_mul(A::load_tw(p.tw_hi, m >> p.tw_shift),
+                                         A::load_tw(p.tw_lo, m & mask));
+            a[q] = A::mul_tw(a[q], w);
+        }
+    }
+
+    double2 *out = reinterpret_cast<double2 *>(p.out) + g0 * p.os[0] + g1 * p.os[1] +
+                   g2 * p.os[2];
+#pragma unroll
+    for (int q = 0; q < E; q++) {
+        C v = p.conj_out ? A::conj(a[q]) : a[q];
+        if (p.scale != 1.0) v = A::scale(v, p.scale);
+        __stcs(out + (int64_t)(j + q * TPL) * p.oes, A::store(v));
+    }
+}
+
+template <class A, int LOG_L, int LOG_B>
+int launch_pass(const tfft_pass &p, cudaStream_t s)
+{
+    constexpr int B = 1 << LOG_B;
+    constexpr size_t smem = pass_smem_bytes<A, LOG_L, B>();
+    static unsigned attr_done = 0; /* one bit per device ordinal */
+    auto kern = pass_kernel<A, LOG_L, B>;
+    if constexpr (smem > 48 * 1024) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        const unsigned bit = 1u << (dev & 31);
+        if (!(attr_done & bit)) {
+            cudaError_t e = cudaFuncSetAttribute(
+                kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) return (int)e;
+            attr_done |= bit;
+        }
+    }
+    const int64_t blocks = (p.n[0] / B) * p.n[1] * p.n[2];
+    if (blocks <= 0) return 0;
+    kern<<<(unsigned)blocks, Shape<LOG_L>::TPL * B, smem, s>>>(p);
+    return (int)cudaGetLastError();
+}
+
+} // namespace tfft

@@ -1,0 +1,112 @@
+/*
+ * Internal C ABI between the C host library (topefft.c, planner.c) and the
+ * CUDA translation units.  Plain C types only: no CUDA or torch types cross
+ * this boundary, so the host side compiles with a plain C compiler.
+ */
+#ifndef TFFT_ABI_H
+#define TFFT_ABI_H
+#include <stddef.h>
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Arithmetic used inside the butterflies.  Storage is FP64 for both. */
+enum tfft_arith {
+    TFFT_ARITH_F64 = 0,  /* native double-precision instructions          */
+    TFFT_ARITH_DF64 = 1, /* double-float: FP32 (hi, lo) pairs on the FP32
+                            pipe; FP64 loads/stores and FP64-accurate tables */
+};
+
+/* Largest line length one CTA transforms (2^13 complex points). */
+#define TFFT_MAX_LOG_L 13
+
+/*
+ * One pass = batched FFTs of length L = 2^log_l over "lines".  Line
+ * (g0, g1, g2) starts at in + g0*is[0] + g1*is[1] + g2*is[2] and its element
+ * i sits at + i*ies (all in complex elements).  The output line is laid out
+ * the same way with os[]/oes, so a pass may transpose on its way out.
+ * A CTA takes b_tile consecutive g0 values (n[0] % b_tile == 0).
+ *
+ * Optional fused extras, applied in this order:
+ *   conj_in   conjugate on load (inverse transforms run as conj(F(conj x)))
+ *   post_tw   multiply output element k of a line by W_N^{t*k}, where t is
+ *             g0 (tw_level 0) or g1 (tw_level 1) and N = tw_n; the factor is
+ *             tw_hi[m >> tw_shift] * tw_lo[m & (2^tw_shift - 1)], m = t*k mod N
+ *   conj_out  conjugate on store
+ *   scale     multiply on store (1.0 = none; 1/N is exact for N = 2^k)
+ */
+typedef struct tfft_pass {
+    int log_l;
+    int b_tile;
+    int arith;
+    int conj_in, conj_out;
+    double scale;
+    const void *in;
+    void *out;
+    int64_t n[3];
+    int64_t is[3], os[3];
+    int64_t ies, oes;
+    const void *tw;      /* W_L^m, m < L, layout per arith */
+    int post_tw;
+    int tw_level;
+    int tw_shift;
+    int64_t tw_n;
+    const void *tw_hi, *tw_lo;
+} tfft_pass;
+
+/* ---- device memory / streams / events (thin wrappers, return 0 or a
+ *      CUDA error code) --------------------------------------------------- */
+int tfft_set_device(int dev);
+int tfft_get_device(int *dev);
+int tfft_device_count(int *n);
+int tfft_malloc(void **p, size_t bytes);
+int tfft_free(void *p);
+int tfft_host_alloc(void **p, size_t bytes);
+int tfft_host_free(void *p);
+int tfft_memset_async(void *p, int v, size_t bytes, void *stream);
+int tfft_h2d(void *dst, const void *src, size_t bytes, void *stream);
+int tfft_d2h(void *dst, const void *src, size_t bytes, void *stream);
+int tfft_d2d(void *dst, const void *src, size_t bytes, void *stream);
+int tfft_stream_create(void **s);
+int tfft_stream_destroy(void *s);
+int tfft_stream_sync(void *s);
+int tfft_event_create(void **e);
+int tfft_event_destroy(void *e);
+int tfft_event_record(void *e, void *stream);
+int tfft_event_elapsed_ns(void *start, void *stop, uint64_t *ns);
+int tfft_last_launch_error(void);
+const char *tfft_error_string(int code);
+
+/* ---- tables --------------------------------------------------------------- */
+/* W_L^m = (cospi(2m/L), -sinpi(2m/L)) for m < L; arith selects double2 or
+ * the double-float layout (float4: re_hi, re_lo, im_hi, im_lo). */
+int tfft_twiddle_table(void *tw, int log_l, int arith, void *stream);
+/* four-step factors: lo[m] = W_N^m (m < 2^shift), hi[h] = W_N^(h<<shift) */
+int tfft_fourstep_tables(void *hi, void *lo, int64_t n, int shift, int arith, void *stream);
+/* rev[g] = bit reversal of g over log2n bits, g < 2^log2n */
+int tfft_bitrev_table(int *rev, int log2n, void *stream);
+/* quarter-wave table of the reference's plan: (cos(2pi k/n), -sin(2pi k/n)),
+ * k < n/4, via sincospi */
+int tfft_quarter_table(void *tw, int n, void *stream);
+/* W_n^m for m < n, any n (DFT path) */
+int tfft_dft_table(void *tw, int n, void *stream);
+
+/* ---- kernels -------------------------------------------------------------- */
+int tfft_launch_pass(const tfft_pass *p, void *stream);
+/* can this (log_l, b_tile, arith) be launched? */
+int tfft_pass_supported(int log_l, int b_tile, int arith);
+/* out[k] = sum_j in[j] W_n^{jk} (dir 1) or conjugate kernel scaled by 1/n */
+int tfft_launch_dft(const void *in, void *out, const void *tw, int n, int dir, void *stream);
+/* in-place bit-reversal permutation of each line of an axis: lines are
+ * (g0, g1) with strides s0, s1; element stride es; uses rev[] */
+int tfft_launch_bitrev_permute(void *data, const int *rev, int log2n, int64_t es,
+                               int64_t n0, int64_t s0, int64_t n1, int64_t s1,
+                               void *stream);
+/* two-point transform in place (the reference's N == 2 case) */
+int tfft_launch_n2(void *data, int dir, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

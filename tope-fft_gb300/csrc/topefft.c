@@ -1,0 +1,1158 @@
+/*
+ * Host side of the GB300 FFT library: the reference's plan / execute /
+ * destroy surface (include/topefft.h) and its extensions (topefft_ext.h),
+ * in C.  Device work goes through the plain-C ABI of tfft_abi.h.
+ *
+ * A plan, whatever its dimensionality, is an array of up to three axes
+ * (x fastest) plus a batch count, resident in device memory, and a list of
+ * passes.  Each axis of length n = 2^lg becomes
+ *   - one pass when lg <= 13 (one CTA transforms a whole line on chip), or
+ *   - two passes (four-step, n = n1*n2) when lg > 13: pass A transforms
+ *     along i2 in place and multiplies by W_n^{i1 k2}; pass B transforms
+ *     along i1 and writes the transposed, natural-order result into the
+ *     plan's second buffer, which then holds the data.
+ * This replaces the reference's swap pass plus one global-memory pass per
+ * radix stage (fft1d.c:41-114, fft2d.c:12-133, fft3d.c:12-213).
+ */
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "../../include/topefft.h"
+#include "../../include/topefft_ext.h"
+#include "tfft_abi.h"
+
+#define TOPE_MAGIC 0x70EFF7u
+#define MAX_PASSES 12
+#define MAX_TABS 16
+
+/* ------------------------------------------------------------------------ */
+/* errors                                                                   */
+/* ------------------------------------------------------------------------ */
+static __thread int g_last_error = TOPE_SUCCESS;
+static __thread int g_last_cuda = 0;
+
+static int set_status(struct topeFFT *f, int st)
+{
+    if (f) f->error = st;
+    if (st != TOPE_SUCCESS) g_last_error = st;
+    return st;
+}
+
+static int cuda_status(struct topeFFT *f, int cuda_rc)
+{
+    if (cuda_rc == 0) return TOPE_SUCCESS;
+    g_last_cuda = cuda_rc;
+    return set_status(f, TOPE_ERR_CUDA);
+}
+
+int topeGetLastError(void)
+{
+    int e = g_last_error;
+    g_last_error = TOPE_SUCCESS;
+    return e;
+}
+
+int topePeekLastError(void) { return g_last_error; }
+int topeLastCudaError(void) { return g_last_cuda; }
+
+const char *topeErrorString(int st)
+{
+    switch (st) {
+    case TOPE_SUCCESS: return "success";
+    case TOPE_ERR_INVALID_SIZE: return "unsupported transform size";
+    case TOPE_ERR_INVALID_ARG: return "invalid argument";
+    case TOPE_ERR_ALLOC: return "allocation failed";
+    case TOPE_ERR_CUDA: return "CUDA call failed";
+    case TOPE_ERR_NOT_INITIALIZED: return "framework not initialised";
+    case TOPE_ERR_DESTROYED: return "plan already destroyed";
+    case TOPE_ERR_UNSUPPORTED: return "operation not supported";
+    case TOPE_ERR_TIMEOUT: return "device-side wait timed out";
+    default: return "unknown status";
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* framework                                                                */
+/* ------------------------------------------------------------------------ */
+typedef struct tope_evpair {
+    void *a, *b;
+} tope_evpair;
+
+typedef struct tope_fw {
+    unsigned magic;
+    void *stream;
+    tope_evpair pair;
+} tope_fw;
+
+uint64_t profileThis(void *event)
+{
+    tope_evpair *p = (tope_evpair *)event;
+    uint64_t ns = 0;
+    if (p && p->a && p->b) tfft_event_elapsed_ns(p->a, p->b, &ns);
+    return ns;
+}
+
+static tope_fw *fw_of(struct topeFFT *f)
+{
+    tope_fw *w = f ? (tope_fw *)f->context : NULL;
+    return (w && w->magic == TOPE_MAGIC) ? w : NULL;
+}
+
+static int fw_open(struct topeFFT *f)
+{
+    int dev = 0, n = 0, rc;
+    const char *ed = getenv("TOPEFFT_DEVICE");
+    rc = tfft_device_count(&n);
+    if (rc || n < 1) return cuda_status(f, rc ? rc : 100 /* cudaErrorNoDevice */);
+    if (ed) dev = atoi(ed);
+    else tfft_get_device(&dev);
+    if (dev < 0 || dev >= n) return set_status(f, TOPE_ERR_INVALID_ARG);
+    if ((rc = tfft_set_device(dev))) return cuda_status(f, rc);
+    tope_fw *w = (tope_fw *)calloc(1, sizeof(tope_fw));
+    if (!w) return set_status(f, TOPE_ERR_ALLOC);
+    if ((rc = tfft_stream_create(&w->stream)) || (rc = tfft_event_create(&w->pair.a)) ||
+        (rc = tfft_event_create(&w->pair.b))) {
+        tfft_event_destroy(w->pair.a);
+        tfft_stream_destroy(w->stream);
+        free(w);
+        return cuda_status(f, rc);
+    }
+    w->magic = TOPE_MAGIC;
+    f->context = w;
+    f->command_queue = w->stream;
+    f->event = &w->pair;
+    f->device_ordinal = dev;
+    f->ret_num_platforms = 1;
+    f->ret_num_devices = (unsigned)n;
+    return TOPE_SUCCESS;
+}
+
+static void fw_close(struct topeFFT *f)
+{
+    tope_fw *w = fw_of(f);
+    if (!w) return;
+    tfft_stream_sync(w->stream);
+    tfft_event_destroy(w->pair.a);
+    tfft_event_destroy(w->pair.b);
+    tfft_stream_destroy(w->stream);
+    w->magic = 0;
+    free(w);
+    f->context = NULL;
+    f->command_queue = NULL;
+    f->event = NULL;
+}
+
+void topeFFTInit(struct topeFFT *f)
+{
+    if (!f) {
+        set_status(NULL, TOPE_ERR_INVALID_ARG);
+        return;
+    }
+    memset(f, 0, sizeof(*f));
+    const char *ea = getenv("TOPEFFT_ARITH");
+    f->arith = (ea && (!strcmp(ea, "df64") || !strcmp(ea, "DF64"))) ? TOPE_ARITH_DF64
+                                                                     : TOPE_ARITH_FP64;
+    set_status(f, fw_open(f));
+}
+
+void topeFFTDestroy(struct topeFFT *f)
+{
+    if (!f) return;
+    fw_close(f);
+    f->live_plans = 0;
+    set_status(f, TOPE_SUCCESS);
+}
+
+void topeSetArith(struct topeFFT *f, int arith)
+{
+    if (!f || (arith != TOPE_ARITH_FP64 && arith != TOPE_ARITH_DF64)) {
+        set_status(f, TOPE_ERR_INVALID_ARG);
+        return;
+    }
+    f->arith = arith;
+    set_status(f, TOPE_SUCCESS);
+}
+
+/* ------------------------------------------------------------------------ */
+/* plan                                                                     */
+/* ------------------------------------------------------------------------ */
+enum { MODE_FFT = 0, MODE_N2 = 1, MODE_DFT = 2 };
+
+typedef struct tope_impl {
+    unsigned magic;
+    int ndim;            /* 1, 2, 3 */
+    int64_t c[4];        /* x, y, z, batch */
+    int64_t st[4];       /* strides in complex elements */
+    int64_t volume;      /* x*y*z: points of one transform */
+    int64_t total;       /* volume * batch */
+    int arith;
+    int mode;
+    void *buf[2];
+    int cur;
+    int npass;
+    tfft_pass pass[MAX_PASSES];
+    int oop[MAX_PASSES];
+    int axis_first[3], axis_count[3];
+    void *tabs[MAX_TABS];
+    int tab_key[MAX_TABS]; /* log_l * 4 + arith for W_L tables, -1 otherwise */
+    int ntabs;
+    int *bitrev[3];
+    void *quarter[3];
+    void *dft_tab;
+    tope_evpair kev, mev;
+    int pending;         /* kev recorded by an async exec, not yet accounted */
+    int last_dir;
+    /* per-launch timing: a pool of event pairs, one per recorded launch */
+    void **pev;
+    int *pev_pass;
+    int pev_cap, pev_used;
+    uint64_t pass_ns[MAX_PASSES], pass_launches[MAX_PASSES];
+} tope_impl;
+
+static int ilog2_exact64(int64_t n)
+{
+    if (n < 1) return -1;
+    int l = 0;
+    while (((int64_t)1 << l) < n) l++;
+    return (((int64_t)1 << l) == n) ? l : -1;
+}
+
+/* reference radix rule (fft1d.c:317-329) and its stage count (:366-369) */
+static int ref_radix(int lg) { return lg % 3 == 0 ? 8 : lg % 2 == 0 ? 4 : 2; }
+static int ref_stages(int lg)
+{
+    int r = ref_radix(lg);
+    return r == 8 ? lg / 3 : r == 4 ? lg / 2 : lg;
+}
+
+static int impl_alloc_tab(tope_impl *P, size_t bytes, int key, void **out)
+{
+    if (P->ntabs >= MAX_TABS) return TOPE_ERR_UNSUPPORTED;
+    int rc = tfft_malloc(out, bytes);
+    if (rc) return TOPE_ERR_ALLOC;
+    P->tabs[P->ntabs] = *out;
+    P->tab_key[P->ntabs] = key;
+    P->ntabs++;
+    return TOPE_SUCCESS;
+}
+
+static size_t tw_elem_bytes(int arith) { (void)arith; return 16; }
+
+/* W_L table shared by every pass of length L */
+static int impl_wl_table(struct topeFFT *f, tope_impl *P, int log_l, const void **out)
+{
+    int key = log_l * 4 + P->arith;
+    for (int i = 0; i < P->ntabs; i++)
+        if (P->tab_key[i] == key) {
+            *out = P->tabs[i];
+            return TOPE_SUCCESS;
+        }
+    void *t;
+    int st = impl_alloc_tab(P, tw_elem_bytes(P->arith) << log_l, key, &t);
+    if (st) return set_status(f, st);
+    int rc = tfft_twiddle_table(t, log_l, P->arith, f->command_queue);
+    if (rc) return cuda_status(f, rc);
+    *out = t;
+    return TOPE_SUCCESS;
+}
+
+/* largest power of two dividing v, capped */
+static int pow2_divisor(int64_t v, int cap)
+{
+    int b = 1;
+    while (b < cap && v % (2 * b) == 0) b *= 2;
+    return b;
+}
+
+/* lines per CTA: about 256 threads, at least 8 adjacent lines when the
+ * line itself is strided (128-byte segments), at most 8192 points per CTA */
+static int choose_b(int log_l, int64_t n0, int strided)
+{
+    int64_t L = (int64_t)1 << log_l;
+    int64_t e = L < 16 ? L : 16;
+    int64_t want = 256 * e / L;
+    if (want < 1) want = 1;
+    if (strided && want < 8) want = 8;
+    int64_t maxb = 8192 / L;
+    if (maxb > 32) maxb = 32;
+    if (want > maxb) want = maxb;
+    if (want < 1) want = 1;
+    return pow2_divisor(n0, (int)want);
+}
+
+typedef struct dimref {
+    int64_t count, in_stride, out_stride;
+    int is_twiddle; /* the four-step index i1 */
+} dimref;
+
+static void sort_dims(dimref *d, int n)
+{
+    for (int i = 1; i < n; i++)
+        for (int j = i; j > 0 && d[j].out_stride < d[j - 1].out_stride; j--) {
+            dimref t = d[j];
+            d[j] = d[j - 1];
+            d[j - 1] = t;
+        }
+}
+
+/* merge neighbours that are contiguous in both input and output */
+static int merge_dims(dimref *d, int n)
+{
+    int m = 0;
+    for (int i = 0; i < n; i++) {
+        if (d[i].count == 1) continue;
+        if (m > 0 && !d[m - 1].is_twiddle && !d[i].is_twiddle &&
+            d[i].in_stride == d[m - 1].in_stride * d[m - 1].count &&
+            d[i].out_stride == d[m - 1].out_stride * d[m - 1].count) {
+            d[m - 1].count *= d[i].count;
+            continue;
+        }
+        d[m++] = d[i];
+    }
+    return m;
+}
+
+static int add_pass(struct topeFFT *f, tope_impl *P, int log_l, int64_t ies, int64_t oes,
+                    dimref *lines, int nl, int oop, int post_tw, int64_t tw_n)
+{
+    if (P->npass >= MAX_PASSES || nl > 3) return set_status(f, TOPE_ERR_UNSUPPORTED);
+    tfft_pass *p = &P->pass[P->npass];
+    memset(p, 0, sizeof(*p));
+    p->log_l = log_l;
+    p->arith = P->arith;
+    p->scale = 1.0;
+    p->ies = ies;
+    p->oes = oes;
+    int lvl_tw = 0;
+    for (int i = 0; i < 3; i++) {
+        if (i < nl) {
+            p->n[i] = lines[i].count;
+            p->is[i] = lines[i].in_stride;
+            p->os[i] = lines[i].out_stride;
+            if (lines[i].is_twiddle) lvl_tw = i;
+        } else {
+            p->n[i] = 1;
+        }
+    }
+    int strided = (ies != 1) || (oes != 1);
+    int b = (nl > 0) ? choose_b(log_l, p->n[0], strided) : 1;
+    p->b_tile = b;
+    if (post_tw) {
+        int lgn = ilog2_exact64(tw_n);
+        int shift = (lgn + 1) / 2;
+        void *hi, *lo;
+        int st = impl_alloc_tab(P, tw_elem_bytes(P->arith) << (lgn - shift), -1, &hi);
+        if (!st) st = impl_alloc_tab(P, tw_elem_bytes(P->arith) << shift, -1, &lo);
+        if (st) return set_status(f, st);
+        int rc = tfft_fourstep_tables(hi, lo, tw_n, shift, P->arith, f->command_queue);
+        if (rc) return cuda_status(f, rc);
+        p->post_tw = 1;
+        p->tw_level = lvl_tw;
+        p->tw_shift = shift;
+        p->tw_n = tw_n;
+        p->tw_hi = hi;
+        p->tw_lo = lo;
+    }
+    if (!tfft_pass_supported(log_l, b, P->arith)) return set_status(f, TOPE_ERR_UNSUPPORTED);
+    int st = impl_wl_table(f, P, log_l, &p->tw);
+    if (st) return st;
+    P->oop[P->npass] = oop;
+    P->npass++;
+    return TOPE_SUCCESS;
+}
+
+/* passes for one axis (0 = x, 1 = y, 2 = z) */
+static int plan_axis(struct topeFFT *f, tope_impl *P, int axis)
+{
+    int64_t n = P->c[axis], s = P->st[axis];
+    int lg = ilog2_exact64(n);
+    P->axis_first[axis] = P->npass;
+    P->axis_count[axis] = 0;
+    if (lg <= 0) return TOPE_SUCCESS; /* length 1: identity */
+    dimref others[4];
+    int no = 0;
+    for (int k = 0; k < 4; k++)
+        if (k != axis && P->c[k] > 1) {
+            others[no].count = P->c[k];
+            others[no].in_stride = others[no].out_stride = P->st[k];
+            others[no].is_twiddle = 0;
+            no++;
+        }
+    int st;
+    if (lg <= TFFT_MAX_LOG_L) {
+        dimref d[4];
+        memcpy(d, others, sizeof(dimref) * no);
+        sort_dims(d, no);
+        int m = merge_dims(d, no);
+        st = add_pass(f, P, lg, s, s, d, m, 0, 0, 0);
+        if (st) return st;
+    } else {
+        if (lg > 2 * TFFT_MAX_LOG_L) return set_status(f, TOPE_ERR_INVALID_SIZE);
+        int l1 = lg / 2, l2 = lg - l1;
+        int64_t n1 = (int64_t)1 << l1, n2 = (int64_t)1 << l2;
+        /* pass A: along i2 (stride s*n1), lines i1 (stride s) x others */
+        dimref d[5];
+        memcpy(d, others, sizeof(dimref) * no);
+        d[no].count = n1;
+        d[no].in_stride = d[no].out_stride = s;
+        d[no].is_twiddle = 1;
+        sort_dims(d, no + 1);
+        int m = merge_dims(d, no + 1);
+        st = add_pass(f, P, l2, s * n1, s * n1, d, m, 0, 1, n);
+        if (st) return st;
+        /* pass B: along i1 (stride s), lines k2 (in s*n1, out s) x others;
+         * element k1 goes to s*(k1*n2 + k2) in the other buffer */
+        memcpy(d, others, sizeof(dimref) * no);
+        d[no].count = n2;
+        d[no].in_stride = s * n1;
+        d[no].out_stride = s;
+        d[no].is_twiddle = 0;
+        sort_dims(d, no + 1);
+        m = merge_dims(d, no + 1);
+        st = add_pass(f, P, l1, s, s * n2, d, m, 1, 0, 0);
+        if (st) return st;
+    }
+    P->axis_count[axis] = P->npass - P->axis_first[axis];
+    return TOPE_SUCCESS;
+}
+
+static void impl_free(tope_impl *P)
+{
+    if (!P) return;
+    for (int i = 0; i < P->ntabs; i++) tfft_free(P->tabs[i]);
+    for (int a = 0; a < 3; a++) {
+        tfft_free(P->bitrev[a]);
+        tfft_free(P->quarter[a]);
+    }
+    tfft_free(P->dft_tab);
+    tfft_free(P->buf[0]);
+    tfft_free(P->buf[1]);
+    tfft_event_destroy(P->kev.a);
+    tfft_event_destroy(P->kev.b);
+    tfft_event_destroy(P->mev.a);
+    tfft_event_destroy(P->mev.b);
+    for (int i = 0; i < 2 * P->pev_cap; i++) tfft_event_destroy(P->pev[i]);
+    free(P->pev);
+    free(P->pev_pass);
+    P->magic = 0;
+    free(P);
+}
+
+/* next event pair of the per-launch pool (grown in chunks); NULL on failure */
+static void **pev_take(tope_impl *P, int pass)
+{
+    if (P->pev_used == P->pev_cap) {
+        int cap = P->pev_cap ? 2 * P->pev_cap : 64;
+        void **ev = (void **)realloc(P->pev, sizeof(void *) * 2 * (size_t)cap);
+        if (!ev) return NULL;
+        P->pev = ev;
+        int *pp = (int *)realloc(P->pev_pass, sizeof(int) * (size_t)cap);
+        if (!pp) return NULL;
+        P->pev_pass = pp;
+        for (int i = 2 * P->pev_cap; i < 2 * cap; i++) {
+            if (tfft_event_create(&P->pev[i])) {
+                for (int j = 2 * P->pev_cap; j < i; j++) tfft_event_destroy(P->pev[j]);
+                return NULL;
+            }
+        }
+        P->pev_cap = cap;
+    }
+    P->pev_pass[P->pev_used] = pass;
+    return &P->pev[2 * P->pev_used++];
+}
+
+/* fold recorded per-launch durations (the stream has been synchronised) */
+static void pev_settle(tope_impl *P)
+{
+    for (int k = 0; k < P->pev_used; k++) {
+        uint64_t ns = 0;
+        tfft_event_elapsed_ns(P->pev[2 * k], P->pev[2 * k + 1], &ns);
+        P->pass_ns[P->pev_pass[k]] += ns;
+        P->pass_launches[P->pev_pass[k]]++;
+    }
+    P->pev_used = 0;
+}
+
+/* Build the device state of a plan and upload d.  Returns a status. */
+static int impl_create(struct topeFFT *f, tope_impl **out, int ndim, int64_t x, int64_t y,
+                       int64_t z, int64_t batch, const double *d, uint64_t *t_pre,
+                       uint64_t *t_mem)
+{
+    *out = NULL;
+    if (!f) return set_status(NULL, TOPE_ERR_INVALID_ARG);
+    if (!fw_of(f)) {
+        int st = fw_open(f);
+        if (st) return st;
+    }
+    if (x < 1 || y < 1 || z < 1 || batch < 1) return set_status(f, TOPE_ERR_INVALID_SIZE);
+    tope_impl *P = (tope_impl *)calloc(1, sizeof(tope_impl));
+    if (!P) return set_status(f, TOPE_ERR_ALLOC);
+    P->magic = TOPE_MAGIC;
+    P->ndim = ndim;
+    P->c[0] = x;
+    P->c[1] = y;
+    P->c[2] = z;
+    P->c[3] = batch;
+    P->st[0] = 1;
+    P->st[1] = x;
+    P->st[2] = x * y;
+    P->st[3] = x * y * z;
+    P->volume = x * y * z;
+    P->total = P->volume * batch;
+    P->arith = f->arith;
+    P->last_dir = FORWARD;
+    int st = TOPE_SUCCESS, rc;
+    void *stream = f->command_queue;
+    tope_fw *w = fw_of(f);
+
+    if ((rc = tfft_event_create(&P->kev.a)) || (rc = tfft_event_create(&P->kev.b)) ||
+        (rc = tfft_event_create(&P->mev.a)) || (rc = tfft_event_create(&P->mev.b))) {
+        impl_free(P);
+        return cuda_status(f, rc);
+    }
+
+    int lgx = ilog2_exact64(x), lgy = ilog2_exact64(y), lgz = ilog2_exact64(z);
+    if (ndim == 1 && x == 2 && batch == 1) P->mode = MODE_N2;
+    else if (ndim == 1 && lgx < 0) P->mode = batch == 1 ? MODE_DFT : -1;
+    else if (lgx < 0 || lgy < 0 || lgz < 0) P->mode = -1;
+    else P->mode = MODE_FFT;
+    if (P->mode < 0) {
+        impl_free(P);
+        return set_status(f, TOPE_ERR_INVALID_SIZE);
+    }
+    if (P->mode == MODE_DFT && x > 46340 * 2) {
+        impl_free(P);
+        return set_status(f, TOPE_ERR_INVALID_SIZE);
+    }
+
+    size_t bytes = (size_t)P->total * 16;
+    if (tfft_malloc(&P->buf[0], bytes)) {
+        impl_free(P);
+        return set_status(f, TOPE_ERR_ALLOC);
+    }
+    tfft_event_record(w->pair.a, stream);
+    tfft_event_record(P->kev.a, stream);
+    if (P->mode == MODE_FFT) {
+        for (int a = 0; a < 3 && !st; a++) st = plan_axis(f, P, a);
+        int need2 = 0;
+        for (int i = 0; i < P->npass; i++) need2 |= P->oop[i];
+        if (!st && need2 && tfft_malloc(&P->buf[1], bytes)) st = set_status(f, TOPE_ERR_ALLOC);
+        /* per-axis bit-reversal and quarter-wave tables of the reference's plan */
+        for (int a = 0; a < ndim && !st; a++) {
+            int lg = ilog2_exact64(P->c[a]);
+            if (tfft_malloc((void **)&P->bitrev[a], sizeof(int) * (size_t)P->c[a])) {
+                st = set_status(f, TOPE_ERR_ALLOC);
+                break;
+            }
+            if ((rc = tfft_bitrev_table(P->bitrev[a], lg, stream))) st = cuda_status(f, rc);
+            if (!st && P->c[a] >= 4) {
+                if (tfft_malloc(&P->quarter[a], 16 * (size_t)(P->c[a] / 4)))
+                    st = set_status(f, TOPE_ERR_ALLOC);
+                else if ((rc = tfft_quarter_table(P->quarter[a], (int)P->c[a], stream)))
+                    st = cuda_status(f, rc);
+            }
+        }
+    } else if (P->mode == MODE_DFT) {
+        if (tfft_malloc(&P->buf[1], bytes) || tfft_malloc(&P->dft_tab, 16 * (size_t)x))
+            st = set_status(f, TOPE_ERR_ALLOC);
+        else if ((rc = tfft_dft_table(P->dft_tab, (int)x, stream)))
+            st = cuda_status(f, rc);
+    }
+    tfft_event_record(P->kev.b, stream);
+    if (!st) {
+        if (d) rc = tfft_h2d(P->buf[0], d, bytes, stream);
+        else rc = tfft_memset_async(P->buf[0], 0, bytes, stream);
+        tfft_event_record(w->pair.b, stream);
+        tfft_event_record(P->mev.b, stream);
+        if (!rc) rc = tfft_stream_sync(stream);
+        if (rc) st = cuda_status(f, rc);
+    }
+    if (st) {
+        tfft_stream_sync(stream);
+        impl_free(P);
+        return st;
+    }
+    uint64_t ns = 0;
+    tfft_event_elapsed_ns(P->kev.a, P->kev.b, &ns);
+    *t_pre += ns;
+    tfft_event_elapsed_ns(P->kev.b, P->mev.b, &ns);
+    *t_mem += ns;
+    f->live_plans++;
+    *out = P;
+    return set_status(f, TOPE_SUCCESS);
+}
+
+static tope_impl *impl_of(struct topeFFT *f, void *impl)
+{
+    tope_impl *P = (tope_impl *)impl;
+    if (!f) {
+        set_status(NULL, TOPE_ERR_INVALID_ARG);
+        return NULL;
+    }
+    if (!P || P->magic != TOPE_MAGIC) {
+        set_status(f, TOPE_ERR_DESTROYED);
+        return NULL;
+    }
+    if (!fw_of(f)) {
+        set_status(f, TOPE_ERR_NOT_INITIALIZED);
+        return NULL;
+    }
+    return P;
+}
+
+/* fold pending async kernel time into *t_kernel (caller has synchronised) */
+static void settle(tope_impl *P, uint64_t *t_kernel)
+{
+    pev_settle(P);
+    if (P->pending) {
+        uint64_t ns = 0;
+        tfft_event_elapsed_ns(P->kev.a, P->kev.b, &ns);
+        *t_kernel += ns;
+        P->pending = 0;
+    }
+}
+
+/* Queue passes [first, first+count) on the current buffer.  conj/scale make
+ * the sequence an inverse when dir == INVERSE. */
+static int run_passes(struct topeFFT *f, tope_impl *P, int first, int count, int dir,
+                      double scale)
+{
+    void *stream = f->command_queue;
+    for (int i = first; i < first + count; i++) {
+        tfft_pass p = P->pass[i];
+        p.in = P->buf[P->cur];
+        p.out = P->oop[i] ? P->buf[1 - P->cur] : P->buf[P->cur];
+        p.conj_in = (dir == INVERSE) && (i == first);
+        p.conj_out = (dir == INVERSE) && (i == first + count - 1);
+        p.scale = (i == first + count - 1) ? scale : 1.0;
+        void **ev = f->pass_timing ? pev_take(P, i) : NULL;
+        if (ev) tfft_event_record(ev[0], stream);
+        int rc = tfft_launch_pass(&p, stream);
+        if (ev) tfft_event_record(ev[1], stream);
+        if (rc) return cuda_status(f, rc);
+        if (P->oop[i]) P->cur = 1 - P->cur;
+    }
+    return TOPE_SUCCESS;
+}
+
+/* queue the whole transform; events bracket the kernels */
+static int impl_exec_async(struct topeFFT *f, tope_impl *P, int dir)
+{
+    void *stream = f->command_queue;
+    int rc, st = TOPE_SUCCESS;
+    if (dir != FORWARD && dir != INVERSE) return set_status(f, TOPE_ERR_INVALID_ARG);
+    P->last_dir = dir;
+    tope_fw *w = fw_of(f);
+    tfft_event_record(P->kev.a, stream);
+    tfft_event_record(w->pair.a, stream);
+    if (P->mode == MODE_FFT) {
+        double scale = dir == INVERSE ? 1.0 / (double)P->volume : 1.0;
+        if (P->npass == 0) {
+            /* all axes of length 1: identity (inverse divides by 1) */
+        } else {
+            st = run_passes(f, P, 0, P->npass, dir, scale);
+        }
+    } else if (P->mode == MODE_N2) {
+        if ((rc = tfft_launch_n2(P->buf[P->cur], dir, stream))) st = cuda_status(f, rc);
+    } else if (P->mode == MODE_DFT) {
+        rc = tfft_launch_dft(P->buf[P->cur], P->buf[1 - P->cur], P->dft_tab, (int)P->c[0], dir,
+                             stream);
+        if (rc) st = cuda_status(f, rc);
+        else P->cur = 1 - P->cur;
+    }
+    tfft_event_record(P->kev.b, stream);
+    tfft_event_record(w->pair.b, stream);
+    P->pending = 1;
+    return st;
+}
+
+/* synchronous: exec, then read back into d (if non-NULL) */
+static int impl_exec(struct topeFFT *f, tope_impl *P, double *d, int dir, uint64_t *t_kernel,
+                     uint64_t *t_mem)
+{
+    void *stream = f->command_queue;
+    int st, rc;
+    if (P->mode == MODE_N2) {
+        /* fft1d.c:16-28 transforms the caller's buffer itself */
+        if (!d) return set_status(f, TOPE_ERR_INVALID_ARG);
+        if ((rc = tfft_h2d(P->buf[P->cur], d, 32, stream))) return cuda_status(f, rc);
+    }
+    st = impl_exec_async(f, P, dir);
+    if (st) {
+        tfft_stream_sync(stream);
+        return st;
+    }
+    if (d) {
+        tfft_event_record(P->mev.a, stream);
+        rc = tfft_d2h(d, P->buf[P->cur], (size_t)P->total * 16, stream);
+        tfft_event_record(P->mev.b, stream);
+        if (rc) {
+            tfft_stream_sync(stream);
+            return cuda_status(f, rc);
+        }
+    }
+    if ((rc = tfft_stream_sync(stream))) return cuda_status(f, rc);
+    settle(P, t_kernel);
+    if (d) {
+        uint64_t ns = 0;
+        tfft_event_elapsed_ns(P->mev.a, P->mev.b, &ns);
+        *t_mem += ns;
+    }
+    return set_status(f, TOPE_SUCCESS);
+}
+
+static int impl_axis(struct topeFFT *f, tope_impl *P, int axis, uint64_t *t_kernel)
+{
+    if (axis >= P->ndim || P->mode != MODE_FFT) return set_status(f, TOPE_ERR_INVALID_ARG);
+    void *stream = f->command_queue;
+    tfft_event_record(P->kev.a, stream);
+    int st = run_passes(f, P, P->axis_first[axis], P->axis_count[axis], P->last_dir, 1.0);
+    tfft_event_record(P->kev.b, stream);
+    int rc = tfft_stream_sync(stream);
+    if (st) return st;
+    if (rc) return cuda_status(f, rc);
+    P->pending = 1;
+    settle(P, t_kernel);
+    return set_status(f, TOPE_SUCCESS);
+}
+
+static int impl_destroy(struct topeFFT *f, tope_impl *P)
+{
+    if (f && f->command_queue) tfft_stream_sync(f->command_queue);
+    impl_free(P);
+    if (f) {
+        if (f->live_plans > 0) f->live_plans--;
+        if (f->live_plans == 0) fw_close(f);
+    }
+    return set_status(f, TOPE_SUCCESS);
+}
+
+static int impl_upload(struct topeFFT *f, tope_impl *P, const double *d, uint64_t *t_mem)
+{
+    if (!d) return set_status(f, TOPE_ERR_INVALID_ARG);
+    void *stream = f->command_queue;
+    tfft_event_record(P->mev.a, stream);
+    int rc = tfft_h2d(P->buf[P->cur], d, (size_t)P->total * 16, stream);
+    tfft_event_record(P->mev.b, stream);
+    if (!rc) rc = tfft_stream_sync(stream);
+    if (rc) return cuda_status(f, rc);
+    uint64_t ns = 0;
+    tfft_event_elapsed_ns(P->mev.a, P->mev.b, &ns);
+    *t_mem += ns;
+    return set_status(f, TOPE_SUCCESS);
+}
+
+static int impl_download(struct topeFFT *f, tope_impl *P, double *d, uint64_t *t_kernel,
+                         uint64_t *t_mem)
+{
+    if (!d) return set_status(f, TOPE_ERR_INVALID_ARG);
+    void *stream = f->command_queue;
+    tfft_event_record(P->mev.a, stream);
+    int rc = tfft_d2h(d, P->buf[P->cur], (size_t)P->total * 16, stream);
+    tfft_event_record(P->mev.b, stream);
+    if (!rc) rc = tfft_stream_sync(stream);
+    if (rc) return cuda_status(f, rc);
+    settle(P, t_kernel);
+    uint64_t ns = 0;
+    tfft_event_elapsed_ns(P->mev.a, P->mev.b, &ns);
+    *t_mem += ns;
+    return set_status(f, TOPE_SUCCESS);
+}
+
+/* ------------------------------------------------------------------------ */
+/* public: 1D                                                               */
+/* ------------------------------------------------------------------------ */
+static void sync_fields_1d(struct topePlan1D *t, tope_impl *P)
+{
+    t->data = P->buf[P->cur];
+    t->scratch = P->buf[1 - P->cur];
+}
+
+static void plan1d(struct topeFFT *f, struct topePlan1D *t, int x, int batch, int type, double *d)
+{
+    if (!t) {
+        set_status(f, TOPE_ERR_INVALID_ARG);
+        return;
+    }
+    memset(t, 0, sizeof(*t));
+    t->x = x;
+    t->type = type;
+    t->dim = 1;
+    if (type != C2C) {
+        set_status(f, TOPE_ERR_UNSUPPORTED);
+        return;
+    }
+    int lg = ilog2_exact64(x);
+    t->radix = lg >= 0 ? ref_radix(lg) : -1;
+    t->log = lg >= 0 ? ref_stages(lg) : 0;
+    tope_impl *P;
+    if (impl_create(f, &P, 1, x, 1, 1, batch, d, &t->totalPreKernel, &t->totalMemory)) return;
+    t->impl = P;
+    t->dataSize = (size_t)P->total * 16;
+    t->bitrev = P->bitrev[0];
+    t->twiddle = P->mode == MODE_DFT ? P->dft_tab : P->quarter[0];
+    sync_fields_1d(t, P);
+}
+
+void tope1DPlanInit(struct topeFFT *f, struct topePlan1D *t, int x, int type, double *d)
+{
+    plan1d(f, t, x, 1, type, d);
+}
+
+void tope1DBatchPlanInit(struct topeFFT *f, struct topePlan1D *t, int x, int batch, int type,
+                         double *d)
+{
+    plan1d(f, t, x, batch, type, d);
+}
+
+void tope1DExec(struct topeFFT *f, struct topePlan1D *t, double *d, int dir)
+{
+    tope_impl *P = t ? impl_of(f, t->impl) : NULL;
+    if (!P) return;
+    impl_exec(f, P, d, dir, &t->totalKernel, &t->totalMemory);
+    sync_fields_1d(t, P);
+}
+
+void tope1DExecDevice(struct topeFFT *f, struct topePlan1D *t, int dir)
+{
+    tope_impl *P = t ? impl_of(f, t->impl) : NULL;
+    if (!P) return;
+    if (impl_exec_async(f, P, dir) == TOPE_SUCCESS) set_status(f, TOPE_SUCCESS);
+    sync_fields_1d(t, P);
+}
+
+void tope1DUpload(struct topeFFT *f, struct topePlan1D *t, const double *d)
+{
+    tope_impl *P = t ? impl_of(f, t->impl) : NULL;
+    if (P) impl_upload(f, P, d, &t->totalMemory);
+}
+
+void tope1DDownload(struct topeFFT *f, struct topePlan1D *t, double *d)
+{
+    tope_impl *P = t ? impl_of(f, t->impl) : NULL;
+    if (P) impl_download(f, P, d, &t->totalKernel, &t->totalMemory);
+}
+
+void tope1DDestroy(struct topeFFT *f, struct topePlan1D *t)
+{
+    tope_impl *P = t ? impl_of(f, t->impl) : NULL;
+    if (!P) return;
+    impl_destroy(f, P);
+    t->impl = NULL;
+    t->data = t->scratch = t->bitrev = t->twiddle = NULL;
+}
+
+/* ------------------------------------------------------------------------ */
+/* public: 2D                                                               */
+/* ------------------------------------------------------------------------ */
+void tope2DPlanInit(struct topeFFT *f, struct topePlan2D *t, int x, int y, int type, double *d)
+{
+    if (!t) {
+        set_status(f, TOPE_ERR_INVALID_ARG);
+        return;
+    }
+    memset(t, 0, sizeof(*t));
+    t->x = x;
+    t->y = y;
+    t->type = type;
+    t->dim = 2;
+    if (type != C2C) {
+        set_status(f, TOPE_ERR_UNSUPPORTED);
+        return;
+    }
+    int lx = ilog2_exact64(x), ly = ilog2_exact64(y);
+    if (lx < 0 || ly < 0) {
+        set_status(f, TOPE_ERR_INVALID_SIZE); /* the reference exits here, fft2d.c:355-362 */
+        return;
+    }
+    t->radX = ref_radix(lx);
+    t->radY = ref_radix(ly);
+    t->logX = ref_stages(lx);
+    t->logY = ref_stages(ly);
+    tope_impl *P;
+    if (impl_create(f, &P, 2, x, y, 1, 1, d, &t->totalPreKernel, &t->totalMemory)) return;
+    t->impl = P;
+    t->dataSize = (size_t)P->total * 16;
+    t->bitX = P->bitrev[0];
+    t->bitY = P->bitrev[1];
+    t->twdX = P->quarter[0];
+    t->twdY = P->quarter[1];
+    t->data = P->buf[P->cur];
+}
+
+void tope2DExec(struct topeFFT *f, struct topePlan2D *t, double *d, int dir)
+{
+    tope_impl *P = t ? impl_of(f, t->impl) : NULL;
+    if (!P) return;
+    impl_exec(f, P, d, dir, &t->totalKernel, &t->totalMemory);
+    t->data = P->buf[P->cur];
+}
+
+void tope2DExecDevice(struct topeFFT *f, struct topePlan2D *t, int dir)
+{
+    tope_impl *P = t ? impl_of(f, t->impl) : NULL;
+    if (!P) return;
+    if (impl_exec_async(f, P, dir) == TOPE_SUCCESS) set_status(f, TOPE_SUCCESS);
+    t->data = P->buf[P->cur];
+}
+
+void tope2DExecX(struct topeFFT *f, struct topePlan2D *t)
+{
+    tope_impl *P = t ? impl_of(f, t->impl) : NULL;
+    if (!P) return;
+    impl_axis(f, P, 0, &t->totalKernel);
+    t->data = P->buf[P->cur];
+}
+
+void tope2DExecY(struct topeFFT *f, struct topePlan2D *t)
+{
+    tope_impl *P = t ? impl_of(f, t->impl) : NULL;
+    if (!P) return;
+    impl_axis(f, P, 1, &t->totalKernel);
+    t->data = P->buf[P->cur];
+}
+
+void tope2DUpload(struct topeFFT *f, struct topePlan2D *t, const double *d)
+{
+    tope_impl *P = t ? impl_of(f, t->impl) : NULL;
+    if (P) impl_upload(f, P, d, &t->totalMemory);
+}
+
+void tope2DDownload(struct topeFFT *f, struct topePlan2D *t, double *d)
+{
+    tope_impl *P = t ? impl_of(f, t->impl) : NULL;
+    if (P) impl_download(f, P, d, &t->totalKernel, &t->totalMemory);
+}
+
+void tope2DDestroy(struct topeFFT *f, struct topePlan2D *t)
+{
+    tope_impl *P = t ? impl_of(f, t->impl) : NULL;
+    if (!P) return;
+    impl_destroy(f, P);
+    t->impl = NULL;
+    t->data = t->bitX = t->bitY = t->twdX = t->twdY = NULL;
+}
+
+/* ------------------------------------------------------------------------ */
+/* public: 3D                                                               */
+/* ------------------------------------------------------------------------ */
+void tope3DPlanInit(struct topeFFT *f, struct topePlan3D *t, int x, int y, int z, int type,
+                    double *d)
+{
+    if (!t) {
+        set_status(f, TOPE_ERR_INVALID_ARG);
+        return;
+    }
+    memset(t, 0, sizeof(*t));
+    t->x = x;
+    t->y = y;
+    t->z = z;
+    t->type = type;
+    t->dim = 3;
+    if (type != C2C) {
+        set_status(f, TOPE_ERR_UNSUPPORTED);
+        return;
+    }
+    int lx = ilog2_exact64(x), ly = ilog2_exact64(y), lz = ilog2_exact64(z);
+    if (lx < 0 || ly < 0 || lz < 0) {
+        set_status(f, TOPE_ERR_INVALID_SIZE); /* fft3d.c:522-533 exits */
+        return;
+    }
+    t->radX = ref_radix(lx);
+    t->radY = ref_radix(ly);
+    t->radZ = ref_radix(lz);
+    t->logX = ref_stages(lx);
+    t->logY = ref_stages(ly);
+    t->logZ = ref_stages(lz);
+    tope_impl *P;
+    if (impl_create(f, &P, 3, x, y, z, 1, d, &t->totalPreKernel, &t->totalMemory)) return;
+    t->impl = P;
+    t->dataSize = (size_t)P->total * 16;
+    t->bitX = P->bitrev[0];
+    t->bitY = P->bitrev[1];
+    t->bitZ = P->bitrev[2];
+    t->twdX = P->quarter[0];
+    t->twdY = P->quarter[1];
+    t->twdZ = P->quarter[2];
+    t->data = P->buf[P->cur];
+}
+
+void tope3DExec(struct topeFFT *f, struct topePlan3D *t, double *d, int dir)
+{
+    tope_impl *P = t ? impl_of(f, t->impl) : NULL;
+    if (!P) return;
+    impl_exec(f, P, d, dir, &t->totalKernel, &t->totalMemory);
+    t->data = P->buf[P->cur];
+}
+
+void tope3DExecDevice(struct topeFFT *f, struct topePlan3D *t, int dir)
+{
+    tope_impl *P = t ? impl_of(f, t->impl) : NULL;
+    if (!P) return;
+    if (impl_exec_async(f, P, dir) == TOPE_SUCCESS) set_status(f, TOPE_SUCCESS);
+    t->data = P->buf[P->cur];
+}
+
+void tope3DExecX(struct topeFFT *f, struct topePlan3D *t)
+{
+    tope_impl *P = t ? impl_of(f, t->impl) : NULL;
+    if (!P) return;
+    impl_axis(f, P, 0, &t->totalKernel);
+    t->data = P->buf[P->cur];
+}
+
+void tope3DExecY(struct topeFFT *f, struct topePlan3D *t)
+{
+    tope_impl *P = t ? impl_of(f, t->impl) : NULL;
+    if (!P) return;
+    impl_axis(f, P, 1, &t->totalKernel);
+    t->data = P->buf[P->cur];
+}
+
+void tope3DExecZ(struct topeFFT *f, struct topePlan3D *t)
+{
+    tope_impl *P = t ? impl_of(f, t->impl) : NULL;
+    if (!P) return;
+    impl_axis(f, P, 2, &t->totalKernel);
+    t->data = P->buf[P->cur];
+}
+
+void tope3DUpload(struct topeFFT *f, struct topePlan3D *t, const double *d)
+{
+    tope_impl *P = t ? impl_of(f, t->impl) : NULL;
+    if (P) impl_upload(f, P, d, &t->totalMemory);
+}
+
+void tope3DDownload(struct topeFFT *f, struct topePlan3D *t, double *d)
+{
+    tope_impl *P = t ? impl_of(f, t->impl) : NULL;
+    if (P) impl_download(f, P, d, &t->totalKernel, &t->totalMemory);
+}
+
+void tope3DBitrevPermute(struct topeFFT *f, struct topePlan3D *t, int axis)
+{
+    tope_impl *P = t ? impl_of(f, t->impl) : NULL;
+    if (!P) return;
+    if (axis < 0 || axis > 2 || P->mode != MODE_FFT || P->c[axis] < 2) {
+        set_status(f, TOPE_ERR_INVALID_ARG);
+        return;
+    }
+    /* lines: the two other axes; g0 the one with the smaller stride */
+    int o[2], k = 0;
+    for (int a = 0; a < 3; a++)
+        if (a != axis) o[k++] = a;
+    int rc = tfft_launch_bitrev_permute(P->buf[P->cur], P->bitrev[axis],
+                                        ilog2_exact64(P->c[axis]), P->st[axis], P->c[o[0]],
+                                        P->st[o[0]], P->c[o[1]], P->st[o[1]], f->command_queue);
+    if (!rc) rc = tfft_stream_sync(f->command_queue);
+    if (rc) cuda_status(f, rc);
+    else set_status(f, TOPE_SUCCESS);
+}
+
+void tope3DDestroy(struct topeFFT *f, struct topePlan3D *t)
+{
+    tope_impl *P = t ? impl_of(f, t->impl) : NULL;
+    if (!P) return;
+    impl_destroy(f, P);
+    t->impl = NULL;
+    t->data = t->bitX = t->bitY = t->bitZ = t->twdX = t->twdY = t->twdZ = NULL;
+}
+
+/* ------------------------------------------------------------------------ */
+/* misc                                                                     */
+/* ------------------------------------------------------------------------ */
+void topeSync(struct topeFFT *f)
+{
+    if (!fw_of(f)) {
+        set_status(f, TOPE_ERR_NOT_INITIALIZED);
+        return;
+    }
+    int rc = tfft_stream_sync(f->command_queue);
+    if (rc) cuda_status(f, rc);
+    else set_status(f, TOPE_SUCCESS);
+}
+
+void topeCopyToHost(struct topeFFT *f, void *dst, const void *src, size_t bytes)
+{
+    if (!fw_of(f) || !dst || !src) {
+        set_status(f, TOPE_ERR_INVALID_ARG);
+        return;
+    }
+    int rc = tfft_d2h(dst, src, bytes, f->command_queue);
+    if (!rc) rc = tfft_stream_sync(f->command_queue);
+    if (rc) cuda_status(f, rc);
+    else set_status(f, TOPE_SUCCESS);
+}
+
+void topeSetPassTiming(struct topeFFT *f, int enable)
+{
+    if (!f) {
+        set_status(NULL, TOPE_ERR_INVALID_ARG);
+        return;
+    }
+    f->pass_timing = enable ? 1 : 0;
+    set_status(f, TOPE_SUCCESS);
+}
+
+int topePassTimes(struct topeFFT *f, void *impl, uint64_t *ns, uint64_t *launches, int max)
+{
+    tope_impl *P = impl_of(f, impl);
+    if (!P) return -1;
+    int rc = tfft_stream_sync(f->command_queue);
+    if (rc) {
+        cuda_status(f, rc);
+        return -1;
+    }
+    pev_settle(P);
+    for (int i = 0; i < P->npass && i < max; i++) {
+        if (ns) ns[i] = P->pass_ns[i];
+        if (launches) launches[i] = P->pass_launches[i];
+    }
+    set_status(f, TOPE_SUCCESS);
+    return P->npass;
+}
+
+void topeResetPassTimes(struct topeFFT *f, void *impl)
+{
+    tope_impl *P = impl_of(f, impl);
+    if (!P) return;
+    tfft_stream_sync(f->command_queue);
+    P->pev_used = 0;
+    memset(P->pass_ns, 0, sizeof(P->pass_ns));
+    memset(P->pass_launches, 0, sizeof(P->pass_launches));
+    set_status(f, TOPE_SUCCESS);
+}
+
+int topePassInfo(struct topeFFT *f, void *impl, int i, int64_t info[6])
+{
+    tope_impl *P = impl_of(f, impl);
+    if (!P || !info) return -1;
+    if (i < 0 || i >= P->npass) {
+        set_status(f, TOPE_ERR_INVALID_ARG);
+        return -1;
+    }
+    const tfft_pass *p = &P->pass[i];
+    int64_t L = (int64_t)1 << p->log_l;
+    int64_t e = L < 16 ? L : 16;
+    info[0] = p->log_l;
+    info[1] = p->b_tile;
+    info[2] = (p->n[0] / p->b_tile) * p->n[1] * p->n[2];
+    info[3] = (L / e) * p->b_tile;
+    info[4] = P->oop[i];
+    info[5] = p->post_tw;
+    set_status(f, TOPE_SUCCESS);
+    return 0;
+}
+
+void *topeHostAlloc(size_t bytes)
+{
+    void *p = NULL;
+    if (tfft_host_alloc(&p, bytes)) {
+        set_status(NULL, TOPE_ERR_ALLOC);
+        return NULL;
+    }
+    return p;
+}
+
+void topeHostFree(void *p) { tfft_host_free(p); }

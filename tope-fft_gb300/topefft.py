@@ -1,0 +1,291 @@
+"""Python mirror of the topeFFT C interface, over libtopefft.so (ctypes).
+
+The functions keep the reference's names and argument meaning
+(src/topefft.h, src/util.c:21, src/fft1d.c:12/303/372, src/fft2d.c:136/319/442,
+src/fft3d.c:216/474/628) so tests read like the reference's own drivers
+(test/1d.c:74-90):
+
+    f = TopeFFT(); topeFFTInit(f)
+    t = TopePlan1D(); tope1DPlanInit(f, t, n, C2C, data)
+    tope1DExec(f, t, data, FORWARD)
+    tope1DDestroy(f, t)
+
+`data` is a C-contiguous float64 numpy array of 2*points values (re, im
+interleaved, x fastest).  There is no fallback: if libtopefft.so is missing
+the import fails.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+C2C, R2C = 1, 0
+FORWARD, INVERSE = 1, 0
+
+TOPE_SUCCESS = 0
+TOPE_ERR_INVALID_SIZE = 1
+TOPE_ERR_INVALID_ARG = 2
+TOPE_ERR_ALLOC = 3
+TOPE_ERR_CUDA = 4
+TOPE_ERR_NOT_INITIALIZED = 5
+TOPE_ERR_DESTROYED = 6
+TOPE_ERR_UNSUPPORTED = 7
+TOPE_ERR_TIMEOUT = 8
+TOPE_ARITH_FP64, TOPE_ARITH_DF64 = 0, 1
+
+LIB_PATH = Path(__file__).resolve().parent / "libtopefft.so"
+
+_vp = C.c_void_p
+_u64 = C.c_uint64
+
+
+class TopeFFT(C.Structure):
+    _fields_ = [("error", C.c_int), ("event", _vp), ("platform_id", _vp), ("device", _vp),
+                ("program1D", _vp), ("program2D", _vp), ("program3D", _vp), ("context", _vp),
+                ("command_queue", _vp), ("ret_num_platforms", C.c_uint),
+                ("ret_num_devices", C.c_uint), ("device_ordinal", C.c_int), ("arith", C.c_int),
+                ("live_plans", C.c_int), ("pass_timing", C.c_int)]
+
+
+class TopePlan1D(C.Structure):
+    _fields_ = [("x", C.c_int), ("log", C.c_int), ("type", C.c_int), ("radix", C.c_int),
+                ("kernel", _vp), ("kernel_bit", _vp), ("kernel_swap", _vp),
+                ("kernel_twid", _vp), ("kernel_div", _vp), ("data", _vp), ("bitrev", _vp),
+                ("twiddle", _vp), ("scratch", _vp), ("dataSize", C.c_size_t),
+                ("totalMemory", _u64), ("totalPreKernel", _u64), ("totalKernel", _u64),
+                ("dim", C.c_uint), ("globalSize", _vp), ("localSize", _vp), ("impl", _vp)]
+
+
+class TopePlan2D(C.Structure):
+    _fields_ = [("x", C.c_int), ("y", C.c_int), ("logX", C.c_int), ("logY", C.c_int),
+                ("type", C.c_int), ("radX", C.c_int), ("radY", C.c_int), ("kernelX", _vp),
+                ("kernelY", _vp), ("kernel_bit", _vp), ("kernel_swap", _vp),
+                ("kernel_twid", _vp), ("kernel_div", _vp), ("data", _vp), ("bitX", _vp),
+                ("bitY", _vp), ("twdX", _vp), ("twdY", _vp), ("dataSize", C.c_size_t),
+                ("totalMemory", _u64), ("totalPreKernel", _u64), ("totalKernel", _u64),
+                ("dim", C.c_uint), ("globalSize", _vp), ("localSize", _vp), ("impl", _vp)]
+
+
+class TopePlan3D(C.Structure):
+    _fields_ = [("x", C.c_int), ("y", C.c_int), ("z", C.c_int), ("logX", C.c_int),
+                ("logY", C.c_int), ("logZ", C.c_int), ("type", C.c_int), ("radX", C.c_int),
+                ("radY", C.c_int), ("radZ", C.c_int), ("kernelX", _vp), ("kernelY", _vp),
+                ("kernelZ", _vp), ("kernel_bit", _vp), ("kernel_swap", _vp),
+                ("kernel_twid", _vp), ("kernel_div", _vp), ("data", _vp), ("bitX", _vp),
+                ("bitY", _vp), ("bitZ", _vp), ("twdX", _vp), ("twdY", _vp), ("twdZ", _vp),
+                ("dataSize", C.c_size_t), ("totalMemory", _u64), ("totalPreKernel", _u64),
+                ("totalKernel", _u64), ("dim", C.c_uint), ("globalSize", _vp),
+                ("localSize", _vp), ("impl", _vp)]
+
+
+_F = C.POINTER(TopeFFT)
+_P1, _P2, _P3 = C.POINTER(TopePlan1D), C.POINTER(TopePlan2D), C.POINTER(TopePlan3D)
+_D = C.POINTER(C.c_double)
+
+# (name, restype, argtypes) of every exported entry point of include/topefft.h
+# and include/topefft_ext.h
+SIGNATURES = [
+    ("profileThis", _u64, [_vp]),
+    ("topeFFTInit", None, [_F]),
+    ("tope1DPlanInit", None, [_F, _P1, C.c_int, C.c_int, _D]),
+    ("tope1DExec", None, [_F, _P1, _D, C.c_int]),
+    ("tope1DDestroy", None, [_F, _P1]),
+    ("tope2DPlanInit", None, [_F, _P2, C.c_int, C.c_int, C.c_int, _D]),
+    ("tope2DExec", None, [_F, _P2, _D, C.c_int]),
+    ("tope2DExecX", None, [_F, _P2]),
+    ("tope2DExecY", None, [_F, _P2]),
+    ("tope2DDestroy", None, [_F, _P2]),
+    ("tope3DPlanInit", None, [_F, _P3, C.c_int, C.c_int, C.c_int, C.c_int, _D]),
+    ("tope3DExec", None, [_F, _P3, _D, C.c_int]),
+    ("tope3DExecX", None, [_F, _P3]),
+    ("tope3DExecY", None, [_F, _P3]),
+    ("tope3DExecZ", None, [_F, _P3]),
+    ("tope3DDestroy", None, [_F, _P3]),
+    ("topeGetLastError", C.c_int, []),
+    ("topePeekLastError", C.c_int, []),
+    ("topeErrorString", C.c_char_p, [C.c_int]),
+    ("topeLastCudaError", C.c_int, []),
+    ("topeSetArith", None, [_F, C.c_int]),
+    ("topeFFTDestroy", None, [_F]),
+    ("tope1DExecDevice", None, [_F, _P1, C.c_int]),
+    ("tope2DExecDevice", None, [_F, _P2, C.c_int]),
+    ("tope3DExecDevice", None, [_F, _P3, C.c_int]),
+    ("tope1DUpload", None, [_F, _P1, _D]),
+    ("tope1DDownload", None, [_F, _P1, _D]),
+    ("tope2DUpload", None, [_F, _P2, _D]),
+    ("tope2DDownload", None, [_F, _P2, _D]),
+    ("tope3DUpload", None, [_F, _P3, _D]),
+    ("tope3DDownload", None, [_F, _P3, _D]),
+    ("topeSync", None, [_F]),
+    ("tope1DBatchPlanInit", None, [_F, _P1, C.c_int, C.c_int, C.c_int, _D]),
+    ("topeCopyToHost", None, [_F, _vp, _vp, C.c_size_t]),
+    ("tope3DBitrevPermute", None, [_F, _P3, C.c_int]),
+    ("topeHostAlloc", _vp, [C.c_size_t]),
+    ("topeHostFree", None, [_vp]),
+    ("topeSetPassTiming", None, [_F, C.c_int]),
+    ("topePassTimes", C.c_int, [_F, _vp, C.POINTER(_u64), C.POINTER(_u64), C.c_int]),
+    ("topeResetPassTimes", None, [_F, _vp]),
+    ("topePassInfo", C.c_int, [_F, _vp, C.c_int, C.POINTER(C.c_int64)]),
+]
+
+
+def load_library(path: Path | str = LIB_PATH) -> C.CDLL:
+    path = Path(path)
+    if not path.exists():
+        raise ImportError(f"{path} is missing: build it first (__graft_entry__.build())")
+    lib = C.CDLL(str(path))
+    for name, res, args in SIGNATURES:
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    return lib
+
+
+lib = load_library()
+
+
+def _ptr(d):
+    if d is None:
+        return None
+    if isinstance(d, np.ndarray):
+        if d.dtype != np.float64 or not d.flags.c_contiguous:
+            raise TypeError("data must be a C-contiguous float64 array")
+        return d.ctypes.data_as(_D)
+    if isinstance(d, int):  # raw host address (pinned buffers)
+        return C.cast(d, _D)
+    raise TypeError("unsupported data argument")
+
+
+def topeFFTInit(f: TopeFFT) -> None:
+    lib.topeFFTInit(C.byref(f))
+
+
+def topeFFTDestroy(f: TopeFFT) -> None:
+    lib.topeFFTDestroy(C.byref(f))
+
+
+def topeSetArith(f: TopeFFT, arith: int) -> None:
+    lib.topeSetArith(C.byref(f), arith)
+
+
+def tope1DPlanInit(f, t, x, type_, d) -> None:
+    lib.tope1DPlanInit(C.byref(f), C.byref(t), x, type_, _ptr(d))
+
+
+def tope1DBatchPlanInit(f, t, x, batch, type_, d) -> None:
+    lib.tope1DBatchPlanInit(C.byref(f), C.byref(t), x, batch, type_, _ptr(d))
+
+
+def tope1DExec(f, t, d, dir_) -> None:
+    lib.tope1DExec(C.byref(f), C.byref(t), _ptr(d), dir_)
+
+
+def tope1DDestroy(f, t) -> None:
+    lib.tope1DDestroy(C.byref(f), C.byref(t))
+
+
+def tope2DPlanInit(f, t, x, y, type_, d) -> None:
+    lib.tope2DPlanInit(C.byref(f), C.byref(t), x, y, type_, _ptr(d))
+
+
+def tope2DExec(f, t, d, dir_) -> None:
+    lib.tope2DExec(C.byref(f), C.byref(t), _ptr(d), dir_)
+
+
+def tope2DExecX(f, t) -> None:
+    lib.tope2DExecX(C.byref(f), C.byref(t))
+
+
+def tope2DExecY(f, t) -> None:
+    lib.tope2DExecY(C.byref(f), C.byref(t))
+
+
+def tope2DDestroy(f, t) -> None:
+    lib.tope2DDestroy(C.byref(f), C.byref(t))
+
+
+def tope3DPlanInit(f, t, x, y, z, type_, d) -> None:
+    lib.tope3DPlanInit(C.byref(f), C.byref(t), x, y, z, type_, _ptr(d))
+
+
+def tope3DExec(f, t, d, dir_) -> None:
+    lib.tope3DExec(C.byref(f), C.byref(t), _ptr(d), dir_)
+
+
+def tope3DExecX(f, t) -> None:
+    lib.tope3DExecX(C.byref(f), C.byref(t))
+
+
+def tope3DExecY(f, t) -> None:
+    lib.tope3DExecY(C.byref(f), C.byref(t))
+
+
+def tope3DExecZ(f, t) -> None:
+    lib.tope3DExecZ(C.byref(f), C.byref(t))
+
+
+def tope3DDestroy(f, t) -> None:
+    lib.tope3DDestroy(C.byref(f), C.byref(t))
+
+
+def tope3DBitrevPermute(f, t, axis) -> None:
+    lib.tope3DBitrevPermute(C.byref(f), C.byref(t), axis)
+
+
+def execDevice(f, t, dir_) -> None:
+    fn = {TopePlan1D: lib.tope1DExecDevice, TopePlan2D: lib.tope2DExecDevice,
+          TopePlan3D: lib.tope3DExecDevice}[type(t)]
+    fn(C.byref(f), C.byref(t), dir_)
+
+
+def upload(f, t, d) -> None:
+    fn = {TopePlan1D: lib.tope1DUpload, TopePlan2D: lib.tope2DUpload,
+          TopePlan3D: lib.tope3DUpload}[type(t)]
+    fn(C.byref(f), C.byref(t), _ptr(d))
+
+
+def download(f, t, d) -> None:
+    fn = {TopePlan1D: lib.tope1DDownload, TopePlan2D: lib.tope2DDownload,
+          TopePlan3D: lib.tope3DDownload}[type(t)]
+    fn(C.byref(f), C.byref(t), _ptr(d))
+
+
+def topeSync(f) -> None:
+    lib.topeSync(C.byref(f))
+
+
+def topeGetLastError() -> int:
+    return lib.topeGetLastError()
+
+
+def topeErrorString(st: int) -> str:
+    return lib.topeErrorString(st).decode()
+
+
+def pass_times(f, t):
+    """Per-pass (total ns, launches) since the last reset, and pass geometry."""
+    ns = (_u64 * 16)()
+    cnt = (_u64 * 16)()
+    n = lib.topePassTimes(C.byref(f), t.impl, ns, cnt, 16)
+    out = []
+    for i in range(max(n, 0)):
+        info = (C.c_int64 * 6)()
+        lib.topePassInfo(C.byref(f), t.impl, i, info)
+        out.append({"ns": int(ns[i]), "launches": int(cnt[i]), "log_l": int(info[0]),
+                    "b_tile": int(info[1]), "ctas": int(info[2]), "threads": int(info[3]),
+                    "out_of_place": int(info[4]), "four_step_twiddle": int(info[5])})
+    return out
+
+
+def copy_to_host(f, dst: np.ndarray, device_ptr: int) -> None:
+    lib.topeCopyToHost(C.byref(f), dst.ctypes.data_as(_vp), device_ptr, dst.nbytes)
+
+
+def check(f: TopeFFT) -> None:
+    """Raise if the last call on f failed."""
+    if f.error != TOPE_SUCCESS:
+        st = f.error
+        raise RuntimeError(f"topeFFT error {st}: {topeErrorString(st)}"
+                           + (f" (CUDA {lib.topeLastCudaError()})" if st == TOPE_ERR_CUDA else ""))
