@@ -304,7 +304,7 @@ def run_gpu(args, wl: dict) -> dict:
         step()
     T.topeSync(f)
     T.topeSetPassTiming(f, 1)
-    T.lib.topeResetPassTimes(ctypes.byref(f), t.impl)
+    T.topeResetPassTimes(f, t)
     sampler = ClockSampler(local)
     sampler.start()
     if dist is not None:

@@ -38,11 +38,14 @@ def T():
     return g.load_package()
 
 
-@pytest.fixture
-def fw(T):
-    """A fresh framework on cuda:0 (GPU tests only)."""
+@pytest.fixture(params=["fp64", "df64"])
+def fw(T, request):
+    """A fresh framework on cuda:0 (GPU tests only), once per butterfly
+    arithmetic: native FP64 and double-float (FP32 pairs)."""
     f = T.TopeFFT()
     T.topeFFTInit(f)
+    T.check(f)
+    T.topeSetArith(f, T.TOPE_ARITH_DF64 if request.param == "df64" else T.TOPE_ARITH_FP64)
     T.check(f)
     yield f
     T.topeFFTDestroy(f)

@@ -68,7 +68,360 @@ struct ArithF64 {
         return __ldg(reinterpret_cast<const double2 *>(tab) + m);
     }
     static __device__ __forceinline__ TW tw_mul(TW a, TW b) { return mul_tw(a, b); }
-    static __device__ __forceinline__ C scale(C a, double s) { return make_double2(a.x * s, a.y * s); }
+
+    /* storage conversion; FP64 needs no tile scaling */
+    static constexpr bool kScaled = false;
+    static __device__ __forceinline__ C load_s(double2 v, int) { return v; }
+    static __device__ __forceinline__ double2 store_s(C v, int, double scale)
+    {
+        return scale != 1.0 ? make_double2(v.x * scale, v.y * scale) : v;
+    }
+};
+
+/* ------------------------------------------------------------------------ */
+/* double-float: a value is an unevaluated sum hi + lo of two FP32 numbers.   */
+/* ------------------------------------------------------------------------ */
+
+/* bit casts usable on host (for CPU checks of the arithmetic) and device */
+__host__ __device__ __forceinline__ unsigned f2u(float f)
+{
+#ifdef __CUDA_ARCH__
+    return __float_as_uint(f);
+#else
+    unsigned u;
+    __builtin_memcpy(&u, &f, 4);
+    return u;
+#endif
+}
+__host__ __device__ __forceinline__ float u2f(unsigned u)
+{
+#ifdef __CUDA_ARCH__
+    return __uint_as_float(u);
+#else
+    float f;
+    __builtin_memcpy(&f, &u, 4);
+    return f;
+#endif
+}
+__host__ __device__ __forceinline__ unsigned long long d2ull(double d)
+{
+#ifdef __CUDA_ARCH__
+    return (unsigned long long)__double_as_longlong(d);
+#else
+    unsigned long long u;
+    __builtin_memcpy(&u, &d, 8);
+    return u;
+#endif
+}
+__host__ __device__ __forceinline__ double ull2d(unsigned long long u)
+{
+#ifdef __CUDA_ARCH__
+    return __longlong_as_double((long long)u);
+#else
+    double d;
+    __builtin_memcpy(&d, &u, 8);
+    return d;
+#endif
+}
+__host__ __device__ __forceinline__ int clz64(unsigned long long v)
+{
+#ifdef __CUDA_ARCH__
+    return __clzll((long long)v);
+#else
+    return v ? __builtin_clzll(v) : 64;
+#endif
+}
+__host__ __device__ __forceinline__ float fmaf_(float a, float b, float c)
+{
+#ifdef __CUDA_ARCH__
+    return __fmaf_rn(a, b, c);
+#else
+    return __builtin_fmaf(a, b, c);
+#endif
+}
+/* a + b, never contracted into an FMA (error-free transforms rely on it) */
+__host__ __device__ __forceinline__ float add_rn(float a, float b)
+{
+#ifdef __CUDA_ARCH__
+    return __fadd_rn(a, b);
+#else
+    volatile float s = a + b;
+    return s;
+#endif
+}
+__host__ __device__ __forceinline__ float sub_rn(float a, float b)
+{
+#ifdef __CUDA_ARCH__
+    return __fsub_rn(a, b);
+#else
+    volatile float s = a - b;
+    return s;
+#endif
+}
+__host__ __device__ __forceinline__ float mul_rn(float a, float b)
+{
+#ifdef __CUDA_ARCH__
+    return __fmul_rn(a, b);
+#else
+    volatile float s = a * b;
+    return s;
+#endif
+}
+
+/* biased FP64 exponent field of v */
+__host__ __device__ __forceinline__ unsigned dexp(double v)
+{
+    return (unsigned)(d2ull(v) >> 52) & 0x7ffu;
+}
+
+/*
+ * v * 2^-delta as a (hi, lo) FP32 pair, with integer operations only (no
+ * FP64 instruction).  hi keeps the top 24 significant bits (truncated), lo
+ * the next 23; the 6 lowest mantissa bits are dropped (relative error below
+ * 2^-46).  Values more than 2^100 below 2^delta become 0: delta is the
+ * tile's largest exponent, so they are far below the tile's rounding level.
+ */
+__host__ __device__ __forceinline__ void split_double(double v, int delta, float &hi, float &lo)
+{
+    const unsigned long long b = d2ull(v);
+    const unsigned hw = (unsigned)(b >> 32), lw = (unsigned)b;
+    const int e = (int)((hw >> 20) & 0x7ffu);
+    const int E = e - 1023 - delta;
+    const unsigned sign = hw & 0x80000000u;
+    if (e == 0 || E < -100) {
+        hi = 0.f;
+        lo = 0.f;
+        return;
+    }
+    hi = u2f(sign | ((unsigned)(E + 127) << 23) | ((hw & 0xfffffu) << 3) | (lw >> 29));
+    const unsigned cexp = (unsigned)(E - 23 + 127) << 23;
+    lo = sub_rn(u2f(sign | cexp | ((lw & 0x1fffffffu) >> 6)), u2f(sign | cexp));
+}
+
+/*
+ * (hi + lo) * 2^delta rounded to the nearest double, with one two-sum on
+ * the FP32 pipe and integer operations for the rest.
+ */
+__host__ __device__ __forceinline__ double join_double(float hi, float lo, int delta)
+{
+    /* renormalise: s + e == hi + lo exactly, |e| <= ulp(s)/2 */
+    const float s = add_rn(hi, lo);
+    const float bb = sub_rn(s, hi);
+    const float e = add_rn(sub_rn(hi, sub_rn(s, bb)), sub_rn(lo, bb));
+    const unsigned sb = f2u(s), eb = f2u(e);
+    if ((sb & 0x7fffffffu) == 0) return 0.0;
+    const int es = (int)((sb >> 23) & 0xffu);
+    /* s = Ms * 2^(es-150); keep everything in units of 2^(es-179) */
+    long long S = (long long)(((sb & 0x7fffffu) | (es ? 0x800000u : 0u))) << 29;
+    if (eb & 0x7fffffffu) {
+        const int ee = (int)((eb >> 23) & 0xffu);
+        const long long Me = (long long)((eb & 0x7fffffu) | (ee ? 0x800000u : 0u));
+        const int d = (es ? es : 1) - (ee ? ee : 1);
+        long long term = d <= 29 ? (Me << (29 - d)) : (d - 29 < 63 ? (Me >> (d - 29)) : 0);
+        S += ((sb ^ eb) & 0x80000000u) ? -term : term;
+    }
+    /* normalise S into [2^52, 2^53) */
+    const int top = 63 - clz64((unsigned long long)S);
+    int exp2 = (es ? es : 1) - 150 - 29 + 52; /* exponent of the unit of S, plus 52 */
+    unsigned long long m;
+    if (top > 52) {
+        const int sh = top - 52;
+        const unsigned long long u = (unsigned long long)S;
+        const unsigned long long half = 1ull << (sh - 1);
+        const unsigned long long rem = u & ((1ull << sh) - 1);
+        m = u >> sh;
+        if (rem > half || (rem == half && (m & 1))) m++;
+        exp2 += sh;
+    } else {
+        m = (unsigned long long)S << (52 - top);
+        exp2 -= 52 - top;
+    }
+    const long long be = (long long)exp2 + delta + 1023;
+    if (be <= 0) return (sb & 0x80000000u) ? -0.0 : 0.0;
+    if (be >= 2047) return ull2d(((unsigned long long)(sb & 0x80000000u) << 32) | 0x7ff0000000000000ull);
+    return ull2d(((unsigned long long)(sb & 0x80000000u) << 32) +
+                 ((unsigned long long)be << 52) + (m - (1ull << 52)));
+}
+
+struct df2 {
+    float h, l;
+};
+
+/* error-free sum: s + e == a + b exactly */
+__host__ __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e)
+{
+    s = add_rn(a, b);
+    const float bb = sub_rn(s, a);
+    e = add_rn(sub_rn(a, sub_rn(s, bb)), sub_rn(b, bb));
+}
+
+/* sum of two pairs, left unnormalised (hi exact sum, lo collects the rest) */
+__host__ __device__ __forceinline__ df2 dadd(df2 x, df2 y)
+{
+    df2 r;
+    float e;
+    two_sum(x.h, y.h, r.h, e);
+    r.l = add_rn(e, add_rn(x.l, y.l));
+    return r;
+}
+__host__ __device__ __forceinline__ df2 dsub(df2 x, df2 y)
+{
+    df2 r;
+    float e;
+    two_sum(x.h, -y.h, r.h, e);
+    r.l = add_rn(e, sub_rn(x.l, y.l));
+    return r;
+}
+/* x * c for a constant pair c */
+__host__ __device__ __forceinline__ df2 dmul(df2 x, df2 c)
+{
+    df2 r;
+    r.h = mul_rn(x.h, c.h);
+    float e = fmaf_(x.h, c.h, -r.h);
+    e = fmaf_(x.h, c.l, e);
+    r.l = fmaf_(x.l, c.h, e);
+    return r;
+}
+/* a*b - c*d of pairs, the result's hi from one exact two-sum */
+__host__ __device__ __forceinline__ df2 ddiffprod(df2 a, df2 b, df2 c, df2 d)
+{
+    const float p1 = mul_rn(a.h, b.h), p2 = mul_rn(c.h, d.h);
+    float t = fmaf_(a.h, b.h, -p1);
+    t = sub_rn(t, fmaf_(c.h, d.h, -p2));
+    df2 r;
+    float e;
+    two_sum(p1, -p2, r.h, e);
+    t = fmaf_(a.h, b.l, t);
+    t = fmaf_(a.l, b.h, t);
+    t = fmaf_(-c.h, d.l, t);
+    t = fmaf_(-c.l, d.h, t);
+    r.l = add_rn(e, t);
+    return r;
+}
+
+/* double-float constants of cos(pi/8), sin(pi/8), sqrt(1/2): hi is the
+ * nearest FP32, lo the nearest FP32 to the remainder (|error| < 7e-16) */
+#define TFFT_DF_C8 {0x1.d906bcp-1f, 0x1.e651a8p-26f}
+#define TFFT_DF_S8 {0x1.87de2ap-2f, 0x1.abaa58p-28f}
+#define TFFT_DF_R2 {0x1.6a09e6p-1f, 0x1.9fcef4p-27f}
+
+struct ArithDF64 {
+    struct C {
+        df2 r, i;
+    };
+    using TW = float4; /* re_hi, re_lo, im_hi, im_lo */
+    using S = float4;
+    static constexpr int kId = 1;
+    static constexpr bool kScaled = true;
+
+    static __host__ __device__ __forceinline__ C load_s(double2 v, int delta)
+    {
+        C c;
+        split_double(v.x, delta, c.r.h, c.r.l);
+        split_double(v.y, delta, c.i.h, c.i.l);
+        return c;
+    }
+    static __host__ __device__ __forceinline__ double2 store_s(C v, int delta, double scale)
+    {
+        int ds = 0;
+        if (scale != 1.0) { /* scale is 2^-k: fold it into the exponent */
+            unsigned long long sb = d2ull(scale);
+            ds = (int)((sb >> 52) & 0x7ff) - 1023;
+        }
+        return make_double2(join_double(v.r.h, v.r.l, delta + ds),
+                            join_double(v.i.h, v.i.l, delta + ds));
+    }
+    static __host__ __device__ __forceinline__ S to_smem(C v) { return make_float4(v.r.h, v.r.l, v.i.h, v.i.l); }
+    static __host__ __device__ __forceinline__ C from_smem(S v)
+    {
+        C c;
+        c.r.h = v.x; c.r.l = v.y; c.i.h = v.z; c.i.l = v.w;
+        return c;
+    }
+    static __host__ __device__ __forceinline__ C add(C a, C b)
+    {
+        C c;
+        c.r = dadd(a.r, b.r);
+        c.i = dadd(a.i, b.i);
+        return c;
+    }
+    static __host__ __device__ __forceinline__ C sub(C a, C b)
+    {
+        C c;
+        c.r = dsub(a.r, b.r);
+        c.i = dsub(a.i, b.i);
+        return c;
+    }
+    static __host__ __device__ __forceinline__ df2 dneg(df2 x) { return df2{-x.h, -x.l}; }
+    static __host__ __device__ __forceinline__ C conj(C a)
+    {
+        a.i = dneg(a.i);
+        return a;
+    }
+    static __host__ __device__ __forceinline__ C neg(C a)
+    {
+        a.r = dneg(a.r);
+        a.i = dneg(a.i);
+        return a;
+    }
+    static __host__ __device__ __forceinline__ C mul_mi(C a)
+    {
+        C c;
+        c.r = a.i;
+        c.i = dneg(a.r);
+        return c;
+    }
+    static __host__ __device__ __forceinline__ C mul_w8(C a)
+    {
+        const df2 r2 = TFFT_DF_R2;
+        C c;
+        c.r = dmul(dadd(a.r, a.i), r2);
+        c.i = dmul(dsub(a.i, a.r), r2);
+        return c;
+    }
+    static __host__ __device__ __forceinline__ C mul_w8_3(C a)
+    {
+        const df2 r2 = TFFT_DF_R2;
+        C c;
+        c.r = dmul(dsub(a.i, a.r), r2);
+        c.i = dneg(dmul(dadd(a.r, a.i), r2));
+        return c;
+    }
+    /* a * (c - i s): re = a.r c + a.i s, im = a.i c - a.r s */
+    template <int K>
+    static __host__ __device__ __forceinline__ C mul_w16(C a)
+    {
+        const df2 c8 = TFFT_DF_C8, s8 = TFFT_DF_S8;
+        const df2 c = K == 1 ? c8 : s8, s = K == 1 ? s8 : c8;
+        C o;
+        o.r = ddiffprod(a.r, c, dneg(a.i), s);
+        o.i = ddiffprod(a.i, c, a.r, s);
+        return o;
+    }
+    static __host__ __device__ __forceinline__ C mul_tw(C a, TW w)
+    {
+        const df2 wr = {w.x, w.y}, wi = {w.z, w.w};
+        C o;
+        o.r = ddiffprod(a.r, wr, a.i, wi);
+        o.i = ddiffprod(a.r, wi, dneg(a.i), wr);
+        return o;
+    }
+    static __device__ __forceinline__ TW load_tw(const void *tab, int64_t m)
+    {
+        return __ldg(reinterpret_cast<const float4 *>(tab) + m);
+    }
+    static __host__ __device__ __forceinline__ TW tw_mul(TW a, TW b)
+    {
+        C x;
+        x.r = df2{a.x, a.y};
+        x.i = df2{a.z, a.w};
+        C y = mul_tw(x, b);
+        /* renormalise table products so later products see |lo| << |hi| */
+        float rh, rl, ih, il;
+        two_sum(y.r.h, y.r.l, rh, rl);
+        two_sum(y.i.h, y.i.l, ih, il);
+        return make_float4(rh, rl, ih, il);
+    }
 };
 
 } // namespace tfft

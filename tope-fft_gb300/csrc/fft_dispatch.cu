@@ -1,0 +1,48 @@
+/*
+ * Launch dispatch of the pass kernel: (arithmetic, log2 L, lines per CTA)
+ * -> the instantiation compiled in one of the fft_inst_*.cu units.
+ * Valid shapes: L = 2^0..2^13, B = 1..32 with L*B <= 8192 (at most 512
+ * threads and 136 KB of shared memory per CTA).
+ */
+#include "fft_pass.cuh"
+
+namespace tfft {
+
+static int ilog2_exact(int v)
+{
+    int l = 0;
+    while ((1 << l) < v) l++;
+    return (1 << l) == v ? l : -1;
+}
+
+static LaunchFn find(int log_l, int b_tile, int arith)
+{
+    const int log_b = ilog2_exact(b_tile);
+    if (log_l < 0 || log_l > TFFT_MAX_LOG_L || log_b < 0 || log_b > kMaxLogB) return nullptr;
+    if (arith == TFFT_ARITH_F64)
+        return log_l <= 9 ? launcher_f64_lo(log_l, log_b) : launcher_f64_hi(log_l, log_b);
+    if (arith == TFFT_ARITH_DF64) {
+        if (log_l <= 4) return launcher_df64_0(log_l, log_b);
+        if (log_l <= 6) return launcher_df64_1(log_l, log_b);
+        if (log_l <= 8) return launcher_df64_2(log_l, log_b);
+        if (log_l <= 9) return launcher_df64_3(log_l, log_b);
+        if (log_l <= 11) return launcher_df64_4(log_l, log_b);
+        return launcher_df64_5(log_l, log_b);
+    }
+    return nullptr;
+}
+
+} // namespace tfft
+
+extern "C" int tfft_pass_supported(int log_l, int b_tile, int arith)
+{
+    return tfft::find(log_l, b_tile, arith) != nullptr;
+}
+
+extern "C" int tfft_launch_pass(const tfft_pass *p, void *stream)
+{
+    tfft::LaunchFn f = tfft::find(p->log_l, p->b_tile, p->arith);
+    if (!f) return (int)cudaErrorInvalidValue;
+    if (p->n[0] % p->b_tile) return (int)cudaErrorInvalidValue;
+    return f(*p, (cudaStream_t)stream);
+}

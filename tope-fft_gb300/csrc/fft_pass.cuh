@@ -22,13 +22,15 @@
  * threads reads or writes B*16 contiguous bytes.
  */
 #pragma once
+#include <utility>
+
 #include "fft_arith.cuh"
 #include "tfft_abi.h"
 
 namespace tfft {
 
 template <class A>
-__device__ __forceinline__ void dft2(typename A::C &a0, typename A::C &a1)
+__host__ __device__ __forceinline__ void dft2(typename A::C &a0, typename A::C &a1)
 {
     typename A::C t = A::sub(a0, a1);
     a0 = A::add(a0, a1);
@@ -36,7 +38,7 @@ __device__ __forceinline__ void dft2(typename A::C &a0, typename A::C &a1)
 }
 
 template <class A>
-__device__ __forceinline__ void dft4(typename A::C &a0, typename A::C &a1,
+__host__ __device__ __forceinline__ void dft4(typename A::C &a0, typename A::C &a1,
                                      typename A::C &a2, typename A::C &a3)
 {
     using C = typename A::C;
@@ -50,7 +52,7 @@ __device__ __forceinline__ void dft4(typename A::C &a0, typename A::C &a1,
 
 /* 8 = 4 (inner, stride-2 inputs) x 2 (outer) */
 template <class A>
-__device__ __forceinline__ void dft8(typename A::C *c)
+__host__ __device__ __forceinline__ void dft8(typename A::C *c)
 {
     using C = typename A::C;
     dft4<A>(c[0], c[2], c[4], c[6]);
@@ -70,7 +72,7 @@ __device__ __forceinline__ void dft8(typename A::C *c)
 
 /* 16 = 4 (inner, stride-4 inputs) x 4 (outer), internal twiddles W16^{n2 k1} */
 template <class A>
-__device__ __forceinline__ void dft16(typename A::C *c)
+__host__ __device__ __forceinline__ void dft16(typename A::C *c)
 {
     using C = typename A::C;
 #pragma unroll
@@ -98,12 +100,34 @@ __device__ __forceinline__ void dft16(typename A::C *c)
 }
 
 template <class A, int R>
-__device__ __forceinline__ void dft(typename A::C *c)
+__host__ __device__ __forceinline__ void dft(typename A::C *c)
 {
     if constexpr (R == 2) dft2<A>(c[0], c[1]);
     else if constexpr (R == 4) dft4<A>(c[0], c[1], c[2], c[3]);
     else if constexpr (R == 8) dft8<A>(c);
     else if constexpr (R == 16) dft16<A>(c);
+}
+
+/* largest biased FP64 exponent over the CTA's tile (NT threads) */
+template <int NT, int E>
+__device__ __forceinline__ unsigned tile_max_exp(const double2 (&raw)[E])
+{
+    unsigned m = 0;
+#pragma unroll
+    for (int q = 0; q < E; q++) m = max(m, max(dexp(raw[q].x), dexp(raw[q].y)));
+    constexpr unsigned mask = NT >= 32 ? 0xffffffffu : ((1u << NT) - 1u);
+    m = __reduce_max_sync(mask, m);
+    if constexpr (NT <= 32) {
+        return m;
+    } else {
+        __shared__ unsigned s_m[NT / 32];
+        if ((threadIdx.x & 31) == 0) s_m[threadIdx.x >> 5] = m;
+        __syncthreads();
+        unsigned r = 0;
+#pragma unroll
+        for (int w = 0; w < NT / 32; w++) r = max(r, s_m[w]);
+        return r;
+    }
 }
 
 /* padded shared-memory index of element p of tile line b */
@@ -225,10 +249,17 @@ __global__ void __launch_bounds__(Shape<LOG_L>::TPL * B)
 
     const double2 *in = reinterpret_cast<const double2 *>(p.in) + g0 * p.is[0] + g1 * p.is[1] +
                         g2 * p.is[2];
+    double2 raw[E];
+#pragma unroll
+    for (int q = 0; q < E; q++) raw[q] = __ldcs(in + (int64_t)(j + q * TPL) * p.ies);
+    /* arithmetics with a narrower exponent range work on the tile scaled by
+     * 2^-delta, delta = the tile's largest FP64 exponent */
+    int delta = 0;
+    if constexpr (A::kScaled) delta = (int)tile_max_exp<TPL * B>(raw) - 1023;
     C a[E];
 #pragma unroll
     for (int q = 0; q < E; q++) {
-        C v = A::load(__ldcs(in + (int64_t)(j + q * TPL) * p.ies));
+        C v = A::load_s(raw[q], delta);
         a[q] = p.conj_in ? A::conj(v) : v;
     }
 
@@ -251,8 +282,7 @@ __global__ void __launch_bounds__(Shape<LOG_L>::TPL * B)
 #pragma unroll
     for (int q = 0; q < E; q++) {
         C v = p.conj_out ? A::conj(a[q]) : a[q];
-        if (p.scale != 1.0) v = A::scale(v, p.scale);
-        __stcs(out + (int64_t)(j + q * TPL) * p.oes, A::store(v));
+        __stcs(out + (int64_t)(j + q * TPL) * p.oes, A::store_s(v, delta, p.scale));
     }
 }
 
@@ -280,4 +310,75 @@ int launch_pass(const tfft_pass &p, cudaStream_t s)
     return (int)cudaGetLastError();
 }
 
+/* launch table over (log2 L, log2 B) with L*B <= 8192 */
+using LaunchFn = int (*)(const tfft_pass &, cudaStream_t);
+constexpr int kMaxLogB = 5;
+
+template <class A, int LOG_L, int LOG_B>
+constexpr LaunchFn pick()
+{
+    if constexpr (LOG_L + LOG_B <= 13) return &launch_pass<A, LOG_L, LOG_B>;
+    else return nullptr;
+}
+
+template <class A, int LOG_L, int... LB>
+constexpr void fill_row(LaunchFn *row, std::integer_sequence<int, LB...>)
+{
+    ((row[LB] = pick<A, LOG_L, LB>()), ...);
+}
+
+template <class A, int... LL>
+struct Table {
+    LaunchFn fn[TFFT_MAX_LOG_L + 1][kMaxLogB + 1];
+    constexpr Table() : fn{}
+    {
+        (fill_row<A, LL>(fn[LL], std::make_integer_sequence<int, kMaxLogB + 1>{}), ...);
+    }
+};
+
+template <class A, int... LL>
+constexpr Table<A, LL...> make_table(std::integer_sequence<int, LL...>)
+{
+    return Table<A, LL...>();
+}
+
+/* the rows LO..LO+sizeof(I)-1 only: one translation unit per range of L
+ * keeps each compile short and lets them run in parallel */
+template <class A, int LO, int... I>
+struct RangeTable {
+    LaunchFn fn[TFFT_MAX_LOG_L + 1][kMaxLogB + 1];
+    constexpr RangeTable() : fn{}
+    {
+        (fill_row<A, LO + I>(fn[LO + I], std::make_integer_sequence<int, kMaxLogB + 1>{}), ...);
+    }
+};
+
+template <class A, int LO, int HI, int... I>
+constexpr RangeTable<A, LO, I...> range_table(std::integer_sequence<int, I...>)
+{
+    return RangeTable<A, LO, I...>();
+}
+
+/* defined by the instantiation units fft_inst_*.cu: launcher for
+ * (arith, log2 L, log2 B) or nullptr */
+LaunchFn launcher_f64_lo(int log_l, int log_b);
+LaunchFn launcher_f64_hi(int log_l, int log_b);
+LaunchFn launcher_df64_0(int log_l, int log_b);
+LaunchFn launcher_df64_1(int log_l, int log_b);
+LaunchFn launcher_df64_2(int log_l, int log_b);
+LaunchFn launcher_df64_3(int log_l, int log_b);
+LaunchFn launcher_df64_4(int log_l, int log_b);
+LaunchFn launcher_df64_5(int log_l, int log_b);
+
 } // namespace tfft
+
+/* one instantiation unit: arith A, rows LO..HI, function NAME */
+#define TFFT_INSTANTIATE(A, LO, HI, NAME)                                                     \
+    namespace tfft {                                                                          \
+    static const auto g_tab_##NAME =                                                          \
+        range_table<A, LO, HI>(std::make_integer_sequence<int, (HI) - (LO) + 1>{});           \
+    LaunchFn NAME(int log_l, int log_b)                                                       \
+    {                                                                                         \
+        return (log_l >= (LO) && log_l <= (HI)) ? g_tab_##NAME.fn[log_l][log_b] : nullptr;    \
+    }                                                                                         \
+    }

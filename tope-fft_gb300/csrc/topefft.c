@@ -558,6 +558,12 @@ static int impl_create(struct topeFFT *f, tope_impl **out, int ndim, int64_t x, 
             st = set_status(f, TOPE_ERR_ALLOC);
         else if ((rc = tfft_dft_table(P->dft_tab, (int)x, stream)))
             st = cuda_status(f, rc);
+    } else if (P->mode == MODE_N2) {
+        /* the two-point plan keeps the reference's one-bit reversal table */
+        if (tfft_malloc((void **)&P->bitrev[0], 2 * sizeof(int)))
+            st = set_status(f, TOPE_ERR_ALLOC);
+        else if ((rc = tfft_bitrev_table(P->bitrev[0], 1, stream)))
+            st = cuda_status(f, rc);
     }
     tfft_event_record(P->kev.b, stream);
     if (!st) {

@@ -170,6 +170,14 @@ def topeSetArith(f: TopeFFT, arith: int) -> None:
     lib.topeSetArith(C.byref(f), arith)
 
 
+def topeSetPassTiming(f: TopeFFT, enable: int) -> None:
+    lib.topeSetPassTiming(C.byref(f), int(enable))
+
+
+def topeResetPassTimes(f: TopeFFT, t) -> None:
+    lib.topeResetPassTimes(C.byref(f), t.impl)
+
+
 def tope1DPlanInit(f, t, x, type_, d) -> None:
     lib.tope1DPlanInit(C.byref(f), C.byref(t), x, type_, _ptr(d))
 
