@@ -98,6 +98,23 @@ void topeResetPassTimes(struct topeFFT *f, void *impl);
  * CTA, out-of-place, four-step twiddle}; returns 0, or -1 if i is out of range. */
 int topePassInfo(struct topeFFT *f, void *impl, int i, int64_t info[6]);
 
+/* ---- allocation-free 1D transform ---------------------------------------- */
+/* No counterpart in the reference.  For callers that must not allocate
+ * device memory while they run (a host framework that owns the memory pool,
+ * a budget fixed at start-up, a path where cudaMalloc's device-wide
+ * synchronisation is not acceptable): transforms n complex FP64 values from
+ * device buffer d_in to device buffer d_out (they may be the same) on
+ * stream, FP64 arithmetic, same direction and scaling rules as tope1DExec.
+ * Its scratch (16 MiB) and tables are static device arrays that every GPU
+ * loading the library holds until exit; nothing is allocated.  n must be a
+ * power of two from 1 to TOPE_NOALLOC_MAX_N, else TOPE_ERR_INVALID_SIZE.
+ * The first call on a device builds the tables and waits for the stream:
+ * make it before any stream capture.  All calls share one scratch array, so
+ * calls whose kernels may overlap on the GPU race: serialise them.
+ * Returns a topeStatus. */
+#define TOPE_NOALLOC_MAX_N (1 << 20)
+int topeExec1DNoAlloc(const double *d_in, double *d_out, int n, int dir, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

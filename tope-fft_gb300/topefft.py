@@ -128,6 +128,7 @@ SIGNATURES = [
     ("topePassTimes", C.c_int, [_F, _vp, C.POINTER(_u64), C.POINTER(_u64), C.c_int]),
     ("topeResetPassTimes", None, [_F, _vp]),
     ("topePassInfo", C.c_int, [_F, _vp, C.c_int, C.POINTER(C.c_int64)]),
+    ("topeExec1DNoAlloc", C.c_int, [_vp, _vp, C.c_int, C.c_int, _vp]),
 ]
 
 
