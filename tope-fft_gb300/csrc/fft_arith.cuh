@@ -183,12 +183,24 @@ __host__ __device__ __forceinline__ unsigned dexp(double v)
  */
 __host__ __device__ __forceinline__ void split_double(double v, int delta, float &hi, float &lo)
 {
-    const unsigned long long b = d2ull(v);
+    unsigned long long b = d2ull(v);
+    int e = (int)((b >> 52) & 0x7ffu);
+    if (e == 0) {
+        /* FP64 subnormal: normalise the significand first */
+        const unsigned long long mant = b & 0xfffffffffffffull;
+        if (!mant) {
+            hi = 0.f;
+            lo = 0.f;
+            return;
+        }
+        const int sh = clz64(mant) - 11;
+        b = (b & 0x8000000000000000ull) | ((mant << sh) & 0xfffffffffffffull);
+        e = 1 - sh;
+    }
     const unsigned hw = (unsigned)(b >> 32), lw = (unsigned)b;
-    const int e = (int)((hw >> 20) & 0x7ffu);
     const int E = e - 1023 - delta;
     const unsigned sign = hw & 0x80000000u;
-    if (e == 0 || E < -100) {
+    if (E < -100) {
         hi = 0.f;
         lo = 0.f;
         return;
@@ -237,7 +249,20 @@ __host__ __device__ __forceinline__ double join_double(float hi, float lo, int d
         exp2 -= 52 - top;
     }
     const long long be = (long long)exp2 + delta + 1023;
-    if (be <= 0) return (sb & 0x80000000u) ? -0.0 : 0.0;
+    if (be <= 0) {
+        /* FP64 subnormal result: shift the 53-bit significand into place,
+         * round to nearest even (a carry into bit 52 yields the smallest
+         * normal, as it should) */
+        const long long sh = 1 - be;
+        unsigned long long r = 0;
+        if (sh <= 53) {
+            const unsigned long long half = 1ull << (sh - 1);
+            const unsigned long long rem = m & ((half << 1) - 1);
+            r = m >> sh;
+            if (rem > half || (rem == half && (r & 1))) r++;
+        }
+        return ull2d(((unsigned long long)(sb & 0x80000000u) << 32) | r);
+    }
     if (be >= 2047) return ull2d(((unsigned long long)(sb & 0x80000000u) << 32) | 0x7ff0000000000000ull);
     return ull2d(((unsigned long long)(sb & 0x80000000u) << 32) +
                  ((unsigned long long)be << 52) + (m - (1ull << 52)));
