@@ -53,6 +53,13 @@ WORKLOADS = {
                "desc": "3D C2C FP64 256^3, forward+inverse, N(0,1) re/im"},
     "1d_4096": {"dims": (4096, 1, 1), "batch": 1,
                 "desc": "1D C2C FP64, N=4096, batch 1, forward+inverse, uniform[-1,1) re/im"},
+    "f32_3d_512": {"dims": (512, 512, 512), "batch": 1, "f32": True,
+                   "desc": "split precision: 3D C2C 512^3, FP32 data, uniform[-1,1) field + "
+                           "Gaussian pulse 1e6 (sigma 4) on the real part, forward+inverse"},
+    "f32_1d_4096x2p14": {"dims": (1 << 14, 1, 1), "batch": 4096, "f32": True,
+                         "desc": "split precision: 1D C2C batched 4096 x 2^14, FP32 data, "
+                                 "uniform field + Gaussian pulse 1e6 (sigma 4) per row, "
+                                 "forward+inverse"},
 }
 METRIC = "C2C GFLOP/s & HBM GB/s vs roofline, FP64 plain vs split-precision at stated rel-L2"
 SEED0 = 0x70E0F0F7
@@ -89,9 +96,23 @@ def splitmix_normal(n_complex: int, seed: int) -> np.ndarray:
     return out
 
 
+def pulse_field(dims, batch, seed=SEED0 + 4, amp=1e6, sigma=4.0) -> np.ndarray:
+    """uniform[-1,1) field plus amp*exp(-r^2/(2 sigma^2)) on the real part,
+    centred on the grid (on each row for batched 1D)."""
+    nx, ny, nz = dims
+    x = splitmix_uniform(nx * ny * nz * batch, seed)
+    g = [np.arange(n, dtype=np.float64) - n // 2 for n in (nz, ny, nx)]
+    p = amp * np.exp(-(g[0][:, None, None] ** 2 + g[1][None, :, None] ** 2 +
+                       g[2][None, None, :] ** 2) / (2 * sigma * sigma)).ravel()
+    x[0::2] += np.tile(p, batch)
+    return x
+
+
 def make_input(wl: dict) -> np.ndarray:
     nx, ny, nz = wl["dims"]
     n = nx * ny * nz * wl["batch"]
+    if wl.get("f32"):
+        return pulse_field(wl["dims"], wl["batch"])
     if ny * nz > 1:
         return splitmix_normal(n, SEED0 + 3)
     return splitmix_uniform(n, SEED0 + 2)
@@ -274,26 +295,39 @@ def run_gpu(args, wl: dict) -> dict:
     batch = wl["batch"]
     n = nx * ny * nz
     total = n * batch
+    f32 = bool(wl.get("f32"))
+    es = 8 if f32 else 16
     x = make_input(wl)
+    xs = x.astype(np.float32) if f32 else x  # what the plan stores
 
     f = T.TopeFFT()
     T.topeFFTInit(f)
     T.check(f)
     T.topeSetArith(f, T.TOPE_ARITH_DF64 if args.arith == "df64" else T.TOPE_ARITH_FP64)
-    d = x.copy()
-    if ny * nz == 1:
-        t = T.TopePlan1D()
-        if batch == 1:
-            T.tope1DPlanInit(f, t, nx, T.C2C, d)
+
+    def make_plan(data, single):
+        if ny * nz == 1:
+            p = T.TopePlan1D()
+            if single:
+                T.tope1DBatchPlanInitF32(f, p, nx, batch, T.C2C, data)
+            elif batch == 1:
+                T.tope1DPlanInit(f, p, nx, T.C2C, data)
+            else:
+                T.tope1DBatchPlanInit(f, p, nx, batch, T.C2C, data)
+        elif nz == 1:
+            p = T.TopePlan2D()
+            (T.tope2DPlanInitF32 if single else T.tope2DPlanInit)(f, p, nx, ny, T.C2C, data)
         else:
-            T.tope1DBatchPlanInit(f, t, nx, batch, T.C2C, d)
-    elif nz == 1:
-        t = T.TopePlan2D()
-        T.tope2DPlanInit(f, t, nx, ny, T.C2C, d)
-    else:
-        t = T.TopePlan3D()
-        T.tope3DPlanInit(f, t, nx, ny, nz, T.C2C, d)
-    T.check(f)
+            p = T.TopePlan3D()
+            (T.tope3DPlanInitF32 if single else T.tope3DPlanInit)(f, p, nx, ny, nz, T.C2C, data)
+        T.check(f)
+        return p
+
+    def destroy(p):
+        {T.TopePlan1D: T.tope1DDestroy, T.TopePlan2D: T.tope2DDestroy,
+         T.TopePlan3D: T.tope3DDestroy}[type(p)](f, p)
+
+    t = make_plan(xs.copy(), f32)
     stream = torch.cuda.ExternalStream(f.command_queue)
 
     def step():
@@ -329,13 +363,36 @@ def run_gpu(args, wl: dict) -> dict:
     launches = sum(p["launches"] for p in passes)
 
     # accuracy after W+K round trips (forward then inverse each step)
-    back = np.empty_like(x)
-    T.download(f, t, back)
-    rt = float(np.sqrt(np.sum((back - x) ** 2) / np.sum(x * x)))
+    back = np.empty_like(xs)
+    (T.downloadF32 if f32 else T.download)(f, t, back)
+    xs64 = xs.astype(np.float64)
+    rt = float(np.sqrt(np.sum((back.astype(np.float64) - xs64) ** 2) / np.sum(xs64 * xs64)))
+    accuracy = None
+    if f32:
+        # one forward transform against the library's own FP64 path on the
+        # FP64 input (before FP32 rounding)
+        T.uploadF32(f, t, xs)
+        T.execF32(f, t, back, T.FORWARD)
+        saved = f.arith
+        T.topeSetArith(f, T.TOPE_ARITH_FP64)
+        ref = x.copy()
+        p64 = make_plan(ref, False)
+        (T.tope1DExec if ny * nz == 1 else T.tope2DExec if nz == 1 else T.tope3DExec)(
+            f, p64, ref, T.FORWARD)
+        T.check(f)
+        destroy(p64)
+        T.topeSetArith(f, saved)
+        got = back.astype(np.float64)
+        accuracy = {"rel_l2_vs_fp64": float(np.sqrt(np.sum((got - ref) ** 2) / np.sum(ref * ref))),
+                    "max_abs_vs_fp64": float(np.max(np.abs(got - ref))),
+                    "max_abs_ref": float(np.max(np.abs(ref))),
+                    "reference": "the library's native-FP64 path on the FP64 input, forward",
+                    "gate": 1e-7}
+        del ref, got
 
     # dominant kernel: the pass with the largest total time
     dom = max(passes, key=lambda p: p["ns"]) if passes else None
-    bytes_per_launch = 2 * 16 * total
+    bytes_per_launch = 2 * es * total
     peak, peak_kind = measured_peaks()
     roof = None
     if dom and dom["launches"]:
@@ -343,7 +400,7 @@ def run_gpu(args, wl: dict) -> dict:
         ach = bytes_per_launch / avg_ns  # bytes/ns == GB/s
         roof = {"bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(ach / peak, 4), "peak_source": peak_kind,
-                "traffic": ncu_traffic(args.workload, args.arith),
+                "traffic": ncu_traffic(args.workload, "f32" if f32 else args.arith),
                 "kernel": f"pass_kernel L=2^{dom['log_l']} B={dom['b_tile']} "
                           f"({dom['ctas']} CTAs x {dom['threads']} threads)",
                 "launch_us": round(avg_ns / 1e3, 2),
@@ -351,15 +408,20 @@ def run_gpu(args, wl: dict) -> dict:
                 "fp64_pipe_tflops_measured": FP64_PIPE_TFLOPS}
 
     # e2e through the C interface with pinned host buffers
-    nbytes = x.nbytes
+    nbytes = xs.nbytes
     hp = T.lib.topeHostAlloc(nbytes)
-    host = np.ctypeslib.as_array((ctypes.c_double * (2 * total)).from_address(hp))
-    host[:] = x
-    exec_fn = {T.TopePlan1D: T.tope1DExec, T.TopePlan2D: T.tope2DExec,
-               T.TopePlan3D: T.tope3DExec}[type(t)]
+    ctype = ctypes.c_float if f32 else ctypes.c_double
+    host = np.ctypeslib.as_array((ctype * (2 * total)).from_address(hp))
+    host[:] = xs
+    if f32:
+        exec_fn, up_fn = T.execF32, T.uploadF32
+    else:
+        exec_fn = {T.TopePlan1D: T.tope1DExec, T.TopePlan2D: T.tope2DExec,
+                   T.TopePlan3D: T.tope3DExec}[type(t)]
+        up_fn = T.upload
 
     def e2e_step():
-        T.upload(f, t, hp)
+        up_fn(f, t, hp)
         exec_fn(f, t, hp, T.FORWARD)
         exec_fn(f, t, hp, T.INVERSE)
 
@@ -376,27 +438,25 @@ def run_gpu(args, wl: dict) -> dict:
                                 device=torch.device("cuda", local))
     T.lib.topeHostFree(hp)
 
-    if ny * nz == 1:
-        T.tope1DDestroy(f, t)
-    elif nz == 1:
-        T.tope2DDestroy(f, t)
-    else:
-        T.tope3DDestroy(f, t)
+    destroy(t)
 
+    arith_desc = ("split precision: FP32 data and butterflies, FP64-accurate hi/lo twiddles"
+                  if f32 else "double-float (FP32 pairs) on FP64 storage" if args.arith == "df64"
+                  else "native FP64")
     res = {
         "metric": METRIC, "value": round(value_gflops, 3), "unit": "GFLOP/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32" if f32 else "f64",
         "data": "synthetic (SplitMix64-seeded)",
-        "config": {"workload": args.workload, "description": wl["desc"],
-                   "arith": "double-float (FP32 pairs) on FP64 storage" if args.arith == "df64"
-                   else "native FP64",
-                   "points": total, "l2": f"inputs larger than L2 ({total * 16 >> 20} MiB array vs "
-                                          f"129 MB L2)" if total * 16 > L2_BYTES else
+        "config": {"workload": args.workload, "description": wl["desc"], "arith": arith_desc,
+                   "points": total, "l2": f"inputs larger than L2 ({total * es >> 20} MiB array vs "
+                                          f"129 MB L2)" if total * es > L2_BYTES else
                    "array fits in L2 (latency-bound size)",
                    "parallelism": f"replicas x{ws}"},
-        "hbm_gbs_effective": round(p_min(n) * 2 * 16 * total * 2 / (ms * 1e-3) / 1e9, 1),
+        "hbm_gbs_effective": round(p_min(n, f32) * 2 * es * total * 2 / (ms * 1e-3) / 1e9, 1),
         "rel_l2_roundtrip": rt,
+        "accuracy": accuracy,
         "roofline": roof,
         "passes": passes,
         "e2e": {"value": round(e2e_val / 1e9, 3), "unit": "GFLOP/s",

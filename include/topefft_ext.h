@@ -74,6 +74,25 @@ void topeSync(struct topeFFT *f);
 void tope1DBatchPlanInit(struct topeFFT *f, struct topePlan1D *t, int x, int batch, int type,
                          double *d);
 
+/* ---- split-precision form: FP32 complex data ----------------------------- */
+/* Same plans and semantics as the FP64 entry points, with interleaved FP32
+ * complex data (half the memory traffic).  Arithmetic is FP32; twiddle
+ * factors and the radix-16 constants are FP64-accurate (hi, lo) FP32 pairs,
+ * generated from FP64 sincospi.  The FP64 Exec/Upload/Download entry
+ * points reject these plans (and the F32 ones reject FP64 plans) with
+ * TOPE_ERR_INVALID_ARG.  Device-resident execution uses tope*DExecDevice. */
+void tope1DBatchPlanInitF32(struct topeFFT *f, struct topePlan1D *t, int x, int batch, int type,
+                            float *d);
+void tope2DPlanInitF32(struct topeFFT *f, struct topePlan2D *t, int x, int y, int type, float *d);
+void tope3DPlanInitF32(struct topeFFT *f, struct topePlan3D *t, int x, int y, int z, int type,
+                       float *d);
+void tope1DExecF32(struct topeFFT *f, struct topePlan1D *t, float *d, int dir);
+void tope2DExecF32(struct topeFFT *f, struct topePlan2D *t, float *d, int dir);
+void tope3DExecF32(struct topeFFT *f, struct topePlan3D *t, float *d, int dir);
+/* impl is the plan's t->impl */
+void topeUploadF32(struct topeFFT *f, void *impl, const float *d);
+void topeDownloadF32(struct topeFFT *f, void *impl, float *d);
+
 /* ---- tables and permutation (plan internals, exposed for inspection) ---- */
 /* Copy a device buffer to host memory (synchronous). */
 void topeCopyToHost(struct topeFFT *f, void *dst, const void *device_src, size_t bytes);

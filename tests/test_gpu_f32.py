@@ -1,0 +1,114 @@
+"""GPU parity of the split-precision form (FP32 data, FP32 butterflies with
+FP64-accurate hi/lo twiddles), through the C interface.
+
+Inputs follow the benchmark configuration of this form: the uniform[-1,1)
+field plus a Gaussian pulse of amplitude 1e6 (sigma = 4 samples per axis)
+added to the real part at the grid centre (per row for batched 1D), which
+stresses dynamic range.  The FP64 oracle runs on the FP64 values before
+they are rounded to FP32.  Gate: rel-L2 <= 1e-7; max-abs is reported.
+"""
+import numpy as np
+import pytest
+
+from conftest import SEED0
+
+pytestmark = pytest.mark.gpu
+
+GATE = 1e-7
+
+
+@pytest.fixture
+def fw(T):
+    """FP32 plans ignore the framework's FP64-storage arithmetic setting, so
+    one framework per test (not one per arithmetic) is enough."""
+    f = T.TopeFFT()
+    T.topeFFTInit(f)
+    T.check(f)
+    yield f
+    T.topeFFTDestroy(f)
+
+
+def pulse_field(orc, dims, batch=1, seed=SEED0 + 4, amp=1e6, sigma=4.0):
+    nx, ny, nz = dims
+    x = orc.uniform(nx * ny * nz * batch, seed)
+    grids = np.meshgrid(*[np.arange(n) - n // 2 for n in (nz, ny, nx)], indexing="ij")
+    r2 = sum(g.astype(np.float64) ** 2 for g, n in zip(grids, (nz, ny, nx)) if n > 1)
+    p = amp * np.exp(-r2 / (2 * sigma * sigma)).ravel()
+    x[0::2] += np.tile(p, batch)
+    return x
+
+
+def run_f32(T, fw, x32, dims, dir_, batch=1):
+    nx, ny, nz = dims
+    d = x32.copy()
+    if ny == 1 and nz == 1:
+        t = T.TopePlan1D()
+        T.tope1DBatchPlanInitF32(fw, t, nx, batch, T.C2C, d)
+    elif nz == 1:
+        t = T.TopePlan2D()
+        T.tope2DPlanInitF32(fw, t, nx, ny, T.C2C, d)
+    else:
+        t = T.TopePlan3D()
+        T.tope3DPlanInitF32(fw, t, nx, ny, nz, T.C2C, d)
+    T.check(fw)
+    T.execF32(fw, t, d, dir_)
+    T.check(fw)
+    {T.TopePlan1D: T.tope1DDestroy, T.TopePlan2D: T.tope2DDestroy,
+     T.TopePlan3D: T.tope3DDestroy}[type(t)](fw, t)
+    return d
+
+
+def oracle_fp64(orc, x, dims, dir_, batch=1):
+    nx, ny, nz = dims
+    return orc.exec(x, nx, ny, nz, dir_, batch=batch)
+
+
+CASES = [((1 << 14, 1, 1), 64), ((1 << 16, 1, 1), 16), ((1 << 20, 1, 1), 1), ((4096, 1, 1), 256),
+         ((512, 512, 1), 1), ((64, 64, 64), 1), ((128, 128, 128), 1), ((32, 64, 128), 1),
+         ((16384, 8, 1), 1), ((8, 8, 16384), 1)]
+
+
+@pytest.mark.parametrize("dims,batch", CASES, ids=lambda c: "x".join(map(str, c)) if isinstance(c, tuple) else str(c))
+def test_f32_error_vs_fp64_oracle(T, fw, orc, dims, batch):
+    x = pulse_field(orc, dims, batch)
+    x32 = x.astype(np.float32)
+    for dir_ in (1, 0):
+        got = run_f32(T, fw, x32, dims, dir_, batch).astype(np.float64)
+        ref = oracle_fp64(orc, x, dims, dir_, batch)
+        err = orc.rel_l2(got, ref)
+        # the algorithm's own error: oracle on the FP32-rounded input
+        ref_r = oracle_fp64(orc, x32.astype(np.float64), dims, dir_, batch)
+        err_alg = orc.rel_l2(got, ref_r)
+        print(f"{dims} x{batch} dir={dir_}: rel-L2 {err:.2e} (vs rounded input {err_alg:.2e}), "
+              f"max-abs {orc.max_abs(got, ref):.3e}")
+        assert err <= GATE and err_alg <= GATE
+
+
+@pytest.mark.parametrize("dims,batch", [((512, 512, 512), 1), ((1 << 14, 1, 1), 4096)],
+                         ids=["512^3", "4096x2^14"])
+def test_f32_full_size(T, fw, orc, dims, batch):
+    """The split-precision benchmark configurations themselves."""
+    x = pulse_field(orc, dims, batch)
+    x32 = x.astype(np.float32)
+    got = run_f32(T, fw, x32, dims, 1, batch).astype(np.float64)
+    ref = oracle_fp64(orc, x, dims, 1, batch)
+    err = orc.rel_l2(got, ref)
+    print(f"{dims} x{batch}: rel-L2 {err:.2e}, max-abs {orc.max_abs(got, ref):.3e}")
+    assert err <= GATE
+
+
+def test_f32_round_trip_and_type_checks(T, fw, orc):
+    n, b = 1 << 15, 8
+    x32 = orc.uniform(n * b, 3).astype(np.float32)
+    d = x32.copy()
+    t = T.TopePlan1D()
+    T.tope1DBatchPlanInitF32(fw, t, n, b, T.C2C, d)
+    T.check(fw)
+    T.execF32(fw, t, d, T.FORWARD)
+    T.execF32(fw, t, d, T.INVERSE)
+    T.check(fw)
+    assert orc.rel_l2(d.astype(np.float64), x32.astype(np.float64)) <= 1e-6
+    T.tope1DExec(fw, t, np.zeros(2 * n * b), T.FORWARD)  # FP64 entry point on an FP32 plan
+    assert fw.error == T.TOPE_ERR_INVALID_ARG
+    T.tope1DDestroy(fw, t)
+    T.check(fw)

@@ -27,6 +27,7 @@ struct ArithF64 {
     using C = double2;
     using TW = double2;
     using S = double2;
+    using Store = double2;
     static constexpr int kId = 0;
 
     static __device__ __forceinline__ C load(double2 v) { return v; }
@@ -336,6 +337,7 @@ struct ArithDF64 {
     };
     using TW = float4; /* re_hi, re_lo, im_hi, im_lo */
     using S = float4;
+    using Store = double2;
     static constexpr int kId = 1;
     static constexpr bool kScaled = true;
 
@@ -446,6 +448,85 @@ struct ArithDF64 {
         two_sum(y.r.h, y.r.l, rh, rl);
         two_sum(y.i.h, y.i.l, ih, il);
         return make_float4(rh, rl, ih, il);
+    }
+};
+
+/* ------------------------------------------------------------------------ */
+/* split precision: FP32 data, FP32 arithmetic, twiddles and the DFT-16      */
+/* constants carried as FP64-accurate (hi, lo) FP32 pairs, so every product */
+/* with an irrational factor has one rounding instead of two.               */
+/* ------------------------------------------------------------------------ */
+struct ArithF32 {
+    using C = float2;
+    using TW = float4; /* re_hi, re_lo, im_hi, im_lo */
+    using S = float2;
+    using Store = float2;
+    static constexpr int kId = 2;
+    static constexpr bool kScaled = false;
+
+    static __host__ __device__ __forceinline__ C load_s(float2 v, int) { return v; }
+    static __host__ __device__ __forceinline__ float2 store_s(C v, int, double scale)
+    {
+        if (scale != 1.0) {
+            const float s = (float)scale; /* a power of two: exact */
+            v.x *= s;
+            v.y *= s;
+        }
+        return v;
+    }
+    static __host__ __device__ __forceinline__ S to_smem(C v) { return v; }
+    static __host__ __device__ __forceinline__ C from_smem(S v) { return v; }
+    static __host__ __device__ __forceinline__ C add(C a, C b) { return make_float2(add_rn(a.x, b.x), add_rn(a.y, b.y)); }
+    static __host__ __device__ __forceinline__ C sub(C a, C b) { return make_float2(sub_rn(a.x, b.x), sub_rn(a.y, b.y)); }
+    static __host__ __device__ __forceinline__ C conj(C a) { return make_float2(a.x, -a.y); }
+    static __host__ __device__ __forceinline__ C neg(C a) { return make_float2(-a.x, -a.y); }
+    static __host__ __device__ __forceinline__ C mul_mi(C a) { return make_float2(a.y, -a.x); }
+    /* x * (ch + cl) with one rounding of the sum of both products */
+    static __host__ __device__ __forceinline__ float mulc(float x, df2 c)
+    {
+        return fmaf_(x, c.h, mul_rn(x, c.l));
+    }
+    static __host__ __device__ __forceinline__ C mul_w8(C a)
+    {
+        const df2 r2 = TFFT_DF_R2;
+        return make_float2(mulc(add_rn(a.x, a.y), r2), mulc(sub_rn(a.y, a.x), r2));
+    }
+    static __host__ __device__ __forceinline__ C mul_w8_3(C a)
+    {
+        const df2 r2 = TFFT_DF_R2;
+        return make_float2(mulc(sub_rn(a.y, a.x), r2), -mulc(add_rn(a.x, a.y), r2));
+    }
+    /* x*c + y*s with c, s as pairs: lo products first, hi products last */
+    static __host__ __device__ __forceinline__ float dot2(float x, df2 c, float y, df2 s)
+    {
+        float t = fmaf_(x, c.l, mul_rn(y, s.l));
+        t = fmaf_(y, s.h, t);
+        return fmaf_(x, c.h, t);
+    }
+    template <int K>
+    static __host__ __device__ __forceinline__ C mul_w16(C a)
+    {
+        const df2 c8 = TFFT_DF_C8, s8 = TFFT_DF_S8;
+        const df2 c = K == 1 ? c8 : s8, s = K == 1 ? s8 : c8;
+        const df2 ns = {-s.h, -s.l};
+        /* re = a.x c + a.y s, im = a.y c - a.x s */
+        return make_float2(dot2(a.x, c, a.y, s), dot2(a.y, c, a.x, ns));
+    }
+    static __host__ __device__ __forceinline__ C mul_tw(C a, TW w)
+    {
+        const df2 wr = {w.x, w.y}, wi = {w.z, w.w};
+        const df2 nwi = {-w.z, -w.w};
+        /* re = a.x wr - a.y wi, im = a.x wi + a.y wr */
+        return make_float2(dot2(a.x, wr, a.y, nwi), dot2(a.x, wi, a.y, wr));
+    }
+    static __device__ __forceinline__ TW load_tw(const void *tab, int64_t m)
+    {
+        return __ldg(reinterpret_cast<const float4 *>(tab) + m);
+    }
+    /* product of two table pairs, kept as a pair */
+    static __host__ __device__ __forceinline__ TW tw_mul(TW a, TW b)
+    {
+        return ArithDF64::tw_mul(a, b);
     }
 };
 

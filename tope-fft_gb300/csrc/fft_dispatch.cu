@@ -19,8 +19,11 @@ static LaunchFn find(int log_l, int b_tile, int arith)
 {
     const int log_b = ilog2_exact(b_tile);
     if (log_l < 0 || log_l > TFFT_MAX_LOG_L || log_b < 0 || log_b > kMaxLogB) return nullptr;
+    if (log_l > TFFT_MAX_LOG_L_ARITH(arith)) return nullptr;
     if (arith == TFFT_ARITH_F64)
         return log_l <= 9 ? launcher_f64_lo(log_l, log_b) : launcher_f64_hi(log_l, log_b);
+    if (arith == TFFT_ARITH_F32)
+        return log_l <= 9 ? launcher_f32_lo(log_l, log_b) : launcher_f32_hi(log_l, log_b);
     if (arith == TFFT_ARITH_DF64) {
         if (log_l <= 4) return launcher_df64_0(log_l, log_b);
         if (log_l <= 6) return launcher_df64_1(log_l, log_b);

@@ -247,13 +247,14 @@ __global__ void __launch_bounds__(Shape<LOG_L>::TPL * B)
     const int64_t rest = blk / tiles0;
     const int64_t g1 = rest % p.n[1], g2 = rest / p.n[1];
 
-    const double2 *in = reinterpret_cast<const double2 *>(p.in) + g0 * p.is[0] + g1 * p.is[1] +
-                        g2 * p.is[2];
-    double2 raw[E];
+    using Store = typename A::Store;
+    const Store *in = reinterpret_cast<const Store *>(p.in) + g0 * p.is[0] + g1 * p.is[1] +
+                      g2 * p.is[2];
+    Store raw[E];
 #pragma unroll
     for (int q = 0; q < E; q++) raw[q] = __ldcs(in + (int64_t)(j + q * TPL) * p.ies);
-    /* arithmetics with a narrower exponent range work on the tile scaled by
-     * 2^-delta, delta = the tile's largest FP64 exponent */
+    /* arithmetics with a narrower exponent range than their storage work on
+     * the tile scaled by 2^-delta, delta = the tile's largest FP64 exponent */
     int delta = 0;
     if constexpr (A::kScaled) delta = (int)tile_max_exp<TPL * B>(raw) - 1023;
     C a[E];
@@ -277,8 +278,8 @@ __global__ void __launch_bounds__(Shape<LOG_L>::TPL * B)
         }
     }
 
-    double2 *out = reinterpret_cast<double2 *>(p.out) + g0 * p.os[0] + g1 * p.os[1] +
-                   g2 * p.os[2];
+    Store *out = reinterpret_cast<Store *>(p.out) + g0 * p.os[0] + g1 * p.os[1] +
+                 g2 * p.os[2];
 #pragma unroll
     for (int q = 0; q < E; q++) {
         C v = p.conj_out ? A::conj(a[q]) : a[q];
@@ -310,14 +311,22 @@ int launch_pass(const tfft_pass &p, cudaStream_t s)
     return (int)cudaGetLastError();
 }
 
-/* launch table over (log2 L, log2 B) with L*B <= 8192 */
+/* launch table over (log2 L, log2 B): at most 512 threads per CTA for
+ * 16-byte elements (L*B <= 8192, 136 KB of shared memory) and 1024 for FP32
+ * complex (L*B <= 16384, 139 KB) */
 using LaunchFn = int (*)(const tfft_pass &, cudaStream_t);
 constexpr int kMaxLogB = 5;
+
+template <class A>
+constexpr int max_log_points()
+{
+    return sizeof(typename A::S) == 8 ? 14 : 13;
+}
 
 template <class A, int LOG_L, int LOG_B>
 constexpr LaunchFn pick()
 {
-    if constexpr (LOG_L + LOG_B <= 13) return &launch_pass<A, LOG_L, LOG_B>;
+    if constexpr (LOG_L + LOG_B <= max_log_points<A>()) return &launch_pass<A, LOG_L, LOG_B>;
     else return nullptr;
 }
 
@@ -369,6 +378,8 @@ LaunchFn launcher_df64_2(int log_l, int log_b);
 LaunchFn launcher_df64_3(int log_l, int log_b);
 LaunchFn launcher_df64_4(int log_l, int log_b);
 LaunchFn launcher_df64_5(int log_l, int log_b);
+LaunchFn launcher_f32_lo(int log_l, int log_b);
+LaunchFn launcher_f32_hi(int log_l, int log_b);
 
 } // namespace tfft
 

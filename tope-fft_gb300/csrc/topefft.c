@@ -187,6 +187,7 @@ typedef struct tope_impl {
     int64_t volume;      /* x*y*z: points of one transform */
     int64_t total;       /* volume * batch */
     int arith;
+    int es;              /* bytes per complex element in memory */
     int mode;
     void *buf[2];
     int cur;
@@ -380,7 +381,8 @@ static int plan_axis(struct topeFFT *f, tope_impl *P, int axis)
             no++;
         }
     int st;
-    if (lg <= TFFT_MAX_LOG_L) {
+    const int max_lg = TFFT_MAX_LOG_L_ARITH(P->arith);
+    if (lg <= max_lg) {
         dimref d[4];
         memcpy(d, others, sizeof(dimref) * no);
         sort_dims(d, no);
@@ -388,7 +390,7 @@ static int plan_axis(struct topeFFT *f, tope_impl *P, int axis)
         st = add_pass(f, P, lg, s, s, d, m, 0, 0, 0);
         if (st) return st;
     } else {
-        if (lg > 2 * TFFT_MAX_LOG_L) return set_status(f, TOPE_ERR_INVALID_SIZE);
+        if (lg > 2 * max_lg) return set_status(f, TOPE_ERR_INVALID_SIZE);
         int l1 = lg / 2, l2 = lg - l1;
         int64_t n1 = (int64_t)1 << l1, n2 = (int64_t)1 << l2;
         /* pass A: along i2 (stride s*n1), lines i1 (stride s) x others */
@@ -474,9 +476,11 @@ static void pev_settle(tope_impl *P)
     P->pev_used = 0;
 }
 
-/* Build the device state of a plan and upload d.  Returns a status. */
+/* Build the device state of a plan and upload d (complex elements of the
+ * arithmetic's storage type; arith < 0 takes the framework's setting).
+ * Returns a status. */
 static int impl_create(struct topeFFT *f, tope_impl **out, int ndim, int64_t x, int64_t y,
-                       int64_t z, int64_t batch, const double *d, uint64_t *t_pre,
+                       int64_t z, int64_t batch, const void *d, int arith, uint64_t *t_pre,
                        uint64_t *t_mem)
 {
     *out = NULL;
@@ -500,7 +504,8 @@ static int impl_create(struct topeFFT *f, tope_impl **out, int ndim, int64_t x, 
     P->st[3] = x * y * z;
     P->volume = x * y * z;
     P->total = P->volume * batch;
-    P->arith = f->arith;
+    P->arith = arith >= 0 ? arith : f->arith;
+    P->es = TFFT_ELEM_BYTES(P->arith);
     P->last_dir = FORWARD;
     int st = TOPE_SUCCESS, rc;
     void *stream = f->command_queue;
@@ -513,8 +518,9 @@ static int impl_create(struct topeFFT *f, tope_impl **out, int ndim, int64_t x, 
     }
 
     int lgx = ilog2_exact64(x), lgy = ilog2_exact64(y), lgz = ilog2_exact64(z);
-    if (ndim == 1 && x == 2 && batch == 1) P->mode = MODE_N2;
-    else if (ndim == 1 && lgx < 0) P->mode = batch == 1 ? MODE_DFT : -1;
+    const int fp64_io = P->es == 16;
+    if (ndim == 1 && x == 2 && batch == 1 && fp64_io) P->mode = MODE_N2;
+    else if (ndim == 1 && lgx < 0) P->mode = (batch == 1 && fp64_io) ? MODE_DFT : -1;
     else if (lgx < 0 || lgy < 0 || lgz < 0) P->mode = -1;
     else P->mode = MODE_FFT;
     if (P->mode < 0) {
@@ -526,7 +532,7 @@ static int impl_create(struct topeFFT *f, tope_impl **out, int ndim, int64_t x, 
         return set_status(f, TOPE_ERR_INVALID_SIZE);
     }
 
-    size_t bytes = (size_t)P->total * 16;
+    size_t bytes = (size_t)P->total * P->es;
     if (tfft_malloc(&P->buf[0], bytes)) {
         impl_free(P);
         return set_status(f, TOPE_ERR_ALLOC);
@@ -673,12 +679,14 @@ static int impl_exec_async(struct topeFFT *f, tope_impl *P, int dir)
     return st;
 }
 
-/* synchronous: exec, then read back into d (if non-NULL) */
-static int impl_exec(struct topeFFT *f, tope_impl *P, double *d, int dir, uint64_t *t_kernel,
-                     uint64_t *t_mem)
+/* synchronous: exec, then read back into d (if non-NULL).  es_caller is the
+ * element size the calling entry point deals in (16 FP64, 8 FP32). */
+static int impl_exec(struct topeFFT *f, tope_impl *P, void *d, int es_caller, int dir,
+                     uint64_t *t_kernel, uint64_t *t_mem)
 {
     void *stream = f->command_queue;
     int st, rc;
+    if (P->es != es_caller) return set_status(f, TOPE_ERR_INVALID_ARG);
     if (P->mode == MODE_N2) {
         /* fft1d.c:16-28 transforms the caller's buffer itself */
         if (!d) return set_status(f, TOPE_ERR_INVALID_ARG);
@@ -691,7 +699,7 @@ static int impl_exec(struct topeFFT *f, tope_impl *P, double *d, int dir, uint64
     }
     if (d) {
         tfft_event_record(P->mev.a, stream);
-        rc = tfft_d2h(d, P->buf[P->cur], (size_t)P->total * 16, stream);
+        rc = tfft_d2h(d, P->buf[P->cur], (size_t)P->total * P->es, stream);
         tfft_event_record(P->mev.b, stream);
         if (rc) {
             tfft_stream_sync(stream);
@@ -734,12 +742,13 @@ static int impl_destroy(struct topeFFT *f, tope_impl *P)
     return set_status(f, TOPE_SUCCESS);
 }
 
-static int impl_upload(struct topeFFT *f, tope_impl *P, const double *d, uint64_t *t_mem)
+static int impl_upload(struct topeFFT *f, tope_impl *P, const void *d, int es_caller,
+                       uint64_t *t_mem)
 {
-    if (!d) return set_status(f, TOPE_ERR_INVALID_ARG);
+    if (!d || P->es != es_caller) return set_status(f, TOPE_ERR_INVALID_ARG);
     void *stream = f->command_queue;
     tfft_event_record(P->mev.a, stream);
-    int rc = tfft_h2d(P->buf[P->cur], d, (size_t)P->total * 16, stream);
+    int rc = tfft_h2d(P->buf[P->cur], d, (size_t)P->total * P->es, stream);
     tfft_event_record(P->mev.b, stream);
     if (!rc) rc = tfft_stream_sync(stream);
     if (rc) return cuda_status(f, rc);
@@ -749,13 +758,13 @@ static int impl_upload(struct topeFFT *f, tope_impl *P, const double *d, uint64_
     return set_status(f, TOPE_SUCCESS);
 }
 
-static int impl_download(struct topeFFT *f, tope_impl *P, double *d, uint64_t *t_kernel,
-                         uint64_t *t_mem)
+static int impl_download(struct topeFFT *f, tope_impl *P, void *d, int es_caller,
+                         uint64_t *t_kernel, uint64_t *t_mem)
 {
-    if (!d) return set_status(f, TOPE_ERR_INVALID_ARG);
+    if (!d || P->es != es_caller) return set_status(f, TOPE_ERR_INVALID_ARG);
     void *stream = f->command_queue;
     tfft_event_record(P->mev.a, stream);
-    int rc = tfft_d2h(d, P->buf[P->cur], (size_t)P->total * 16, stream);
+    int rc = tfft_d2h(d, P->buf[P->cur], (size_t)P->total * P->es, stream);
     tfft_event_record(P->mev.b, stream);
     if (!rc) rc = tfft_stream_sync(stream);
     if (rc) return cuda_status(f, rc);
@@ -775,7 +784,8 @@ static void sync_fields_1d(struct topePlan1D *t, tope_impl *P)
     t->scratch = P->buf[1 - P->cur];
 }
 
-static void plan1d(struct topeFFT *f, struct topePlan1D *t, int x, int batch, int type, double *d)
+static void plan1d(struct topeFFT *f, struct topePlan1D *t, int x, int batch, int type,
+                   const void *d, int arith)
 {
     if (!t) {
         set_status(f, TOPE_ERR_INVALID_ARG);
@@ -793,9 +803,10 @@ static void plan1d(struct topeFFT *f, struct topePlan1D *t, int x, int batch, in
     t->radix = lg >= 0 ? ref_radix(lg) : -1;
     t->log = lg >= 0 ? ref_stages(lg) : 0;
     tope_impl *P;
-    if (impl_create(f, &P, 1, x, 1, 1, batch, d, &t->totalPreKernel, &t->totalMemory)) return;
+    if (impl_create(f, &P, 1, x, 1, 1, batch, d, arith, &t->totalPreKernel, &t->totalMemory))
+        return;
     t->impl = P;
-    t->dataSize = (size_t)P->total * 16;
+    t->dataSize = (size_t)P->total * P->es;
     t->bitrev = P->bitrev[0];
     t->twiddle = P->mode == MODE_DFT ? P->dft_tab : P->quarter[0];
     sync_fields_1d(t, P);
@@ -803,20 +814,34 @@ static void plan1d(struct topeFFT *f, struct topePlan1D *t, int x, int batch, in
 
 void tope1DPlanInit(struct topeFFT *f, struct topePlan1D *t, int x, int type, double *d)
 {
-    plan1d(f, t, x, 1, type, d);
+    plan1d(f, t, x, 1, type, d, -1);
 }
 
 void tope1DBatchPlanInit(struct topeFFT *f, struct topePlan1D *t, int x, int batch, int type,
                          double *d)
 {
-    plan1d(f, t, x, batch, type, d);
+    plan1d(f, t, x, batch, type, d, -1);
+}
+
+void tope1DBatchPlanInitF32(struct topeFFT *f, struct topePlan1D *t, int x, int batch, int type,
+                            float *d)
+{
+    plan1d(f, t, x, batch, type, d, TFFT_ARITH_F32);
+}
+
+void tope1DExecF32(struct topeFFT *f, struct topePlan1D *t, float *d, int dir)
+{
+    tope_impl *P = t ? impl_of(f, t->impl) : NULL;
+    if (!P) return;
+    impl_exec(f, P, d, 8, dir, &t->totalKernel, &t->totalMemory);
+    sync_fields_1d(t, P);
 }
 
 void tope1DExec(struct topeFFT *f, struct topePlan1D *t, double *d, int dir)
 {
     tope_impl *P = t ? impl_of(f, t->impl) : NULL;
     if (!P) return;
-    impl_exec(f, P, d, dir, &t->totalKernel, &t->totalMemory);
+    impl_exec(f, P, d, 16, dir, &t->totalKernel, &t->totalMemory);
     sync_fields_1d(t, P);
 }
 
@@ -831,13 +856,13 @@ void tope1DExecDevice(struct topeFFT *f, struct topePlan1D *t, int dir)
 void tope1DUpload(struct topeFFT *f, struct topePlan1D *t, const double *d)
 {
     tope_impl *P = t ? impl_of(f, t->impl) : NULL;
-    if (P) impl_upload(f, P, d, &t->totalMemory);
+    if (P) impl_upload(f, P, d, 16, &t->totalMemory);
 }
 
 void tope1DDownload(struct topeFFT *f, struct topePlan1D *t, double *d)
 {
     tope_impl *P = t ? impl_of(f, t->impl) : NULL;
-    if (P) impl_download(f, P, d, &t->totalKernel, &t->totalMemory);
+    if (P) impl_download(f, P, d, 16, &t->totalKernel, &t->totalMemory);
 }
 
 void tope1DDestroy(struct topeFFT *f, struct topePlan1D *t)
@@ -852,7 +877,8 @@ void tope1DDestroy(struct topeFFT *f, struct topePlan1D *t)
 /* ------------------------------------------------------------------------ */
 /* public: 2D                                                               */
 /* ------------------------------------------------------------------------ */
-void tope2DPlanInit(struct topeFFT *f, struct topePlan2D *t, int x, int y, int type, double *d)
+static void plan2d(struct topeFFT *f, struct topePlan2D *t, int x, int y, int type,
+                   const void *d, int arith)
 {
     if (!t) {
         set_status(f, TOPE_ERR_INVALID_ARG);
@@ -877,9 +903,9 @@ void tope2DPlanInit(struct topeFFT *f, struct topePlan2D *t, int x, int y, int t
     t->logX = ref_stages(lx);
     t->logY = ref_stages(ly);
     tope_impl *P;
-    if (impl_create(f, &P, 2, x, y, 1, 1, d, &t->totalPreKernel, &t->totalMemory)) return;
+    if (impl_create(f, &P, 2, x, y, 1, 1, d, arith, &t->totalPreKernel, &t->totalMemory)) return;
     t->impl = P;
-    t->dataSize = (size_t)P->total * 16;
+    t->dataSize = (size_t)P->total * P->es;
     t->bitX = P->bitrev[0];
     t->bitY = P->bitrev[1];
     t->twdX = P->quarter[0];
@@ -887,11 +913,29 @@ void tope2DPlanInit(struct topeFFT *f, struct topePlan2D *t, int x, int y, int t
     t->data = P->buf[P->cur];
 }
 
+void tope2DPlanInit(struct topeFFT *f, struct topePlan2D *t, int x, int y, int type, double *d)
+{
+    plan2d(f, t, x, y, type, d, -1);
+}
+
+void tope2DPlanInitF32(struct topeFFT *f, struct topePlan2D *t, int x, int y, int type, float *d)
+{
+    plan2d(f, t, x, y, type, d, TFFT_ARITH_F32);
+}
+
+void tope2DExecF32(struct topeFFT *f, struct topePlan2D *t, float *d, int dir)
+{
+    tope_impl *P = t ? impl_of(f, t->impl) : NULL;
+    if (!P) return;
+    impl_exec(f, P, d, 8, dir, &t->totalKernel, &t->totalMemory);
+    t->data = P->buf[P->cur];
+}
+
 void tope2DExec(struct topeFFT *f, struct topePlan2D *t, double *d, int dir)
 {
     tope_impl *P = t ? impl_of(f, t->impl) : NULL;
     if (!P) return;
-    impl_exec(f, P, d, dir, &t->totalKernel, &t->totalMemory);
+    impl_exec(f, P, d, 16, dir, &t->totalKernel, &t->totalMemory);
     t->data = P->buf[P->cur];
 }
 
@@ -922,13 +966,13 @@ void tope2DExecY(struct topeFFT *f, struct topePlan2D *t)
 void tope2DUpload(struct topeFFT *f, struct topePlan2D *t, const double *d)
 {
     tope_impl *P = t ? impl_of(f, t->impl) : NULL;
-    if (P) impl_upload(f, P, d, &t->totalMemory);
+    if (P) impl_upload(f, P, d, 16, &t->totalMemory);
 }
 
 void tope2DDownload(struct topeFFT *f, struct topePlan2D *t, double *d)
 {
     tope_impl *P = t ? impl_of(f, t->impl) : NULL;
-    if (P) impl_download(f, P, d, &t->totalKernel, &t->totalMemory);
+    if (P) impl_download(f, P, d, 16, &t->totalKernel, &t->totalMemory);
 }
 
 void tope2DDestroy(struct topeFFT *f, struct topePlan2D *t)
@@ -943,8 +987,8 @@ void tope2DDestroy(struct topeFFT *f, struct topePlan2D *t)
 /* ------------------------------------------------------------------------ */
 /* public: 3D                                                               */
 /* ------------------------------------------------------------------------ */
-void tope3DPlanInit(struct topeFFT *f, struct topePlan3D *t, int x, int y, int z, int type,
-                    double *d)
+static void plan3d(struct topeFFT *f, struct topePlan3D *t, int x, int y, int z, int type,
+                   const void *d, int arith)
 {
     if (!t) {
         set_status(f, TOPE_ERR_INVALID_ARG);
@@ -972,9 +1016,9 @@ void tope3DPlanInit(struct topeFFT *f, struct topePlan3D *t, int x, int y, int z
     t->logY = ref_stages(ly);
     t->logZ = ref_stages(lz);
     tope_impl *P;
-    if (impl_create(f, &P, 3, x, y, z, 1, d, &t->totalPreKernel, &t->totalMemory)) return;
+    if (impl_create(f, &P, 3, x, y, z, 1, d, arith, &t->totalPreKernel, &t->totalMemory)) return;
     t->impl = P;
-    t->dataSize = (size_t)P->total * 16;
+    t->dataSize = (size_t)P->total * P->es;
     t->bitX = P->bitrev[0];
     t->bitY = P->bitrev[1];
     t->bitZ = P->bitrev[2];
@@ -984,11 +1028,45 @@ void tope3DPlanInit(struct topeFFT *f, struct topePlan3D *t, int x, int y, int z
     t->data = P->buf[P->cur];
 }
 
+void tope3DPlanInit(struct topeFFT *f, struct topePlan3D *t, int x, int y, int z, int type,
+                    double *d)
+{
+    plan3d(f, t, x, y, z, type, d, -1);
+}
+
+void tope3DPlanInitF32(struct topeFFT *f, struct topePlan3D *t, int x, int y, int z, int type,
+                       float *d)
+{
+    plan3d(f, t, x, y, z, type, d, TFFT_ARITH_F32);
+}
+
+void tope3DExecF32(struct topeFFT *f, struct topePlan3D *t, float *d, int dir)
+{
+    tope_impl *P = t ? impl_of(f, t->impl) : NULL;
+    if (!P) return;
+    impl_exec(f, P, d, 8, dir, &t->totalKernel, &t->totalMemory);
+    t->data = P->buf[P->cur];
+}
+
+void topeUploadF32(struct topeFFT *f, void *impl, const float *d)
+{
+    tope_impl *P = impl_of(f, impl);
+    uint64_t ns = 0;
+    if (P) impl_upload(f, P, d, 8, &ns);
+}
+
+void topeDownloadF32(struct topeFFT *f, void *impl, float *d)
+{
+    tope_impl *P = impl_of(f, impl);
+    uint64_t k = 0, m = 0;
+    if (P) impl_download(f, P, d, 8, &k, &m);
+}
+
 void tope3DExec(struct topeFFT *f, struct topePlan3D *t, double *d, int dir)
 {
     tope_impl *P = t ? impl_of(f, t->impl) : NULL;
     if (!P) return;
-    impl_exec(f, P, d, dir, &t->totalKernel, &t->totalMemory);
+    impl_exec(f, P, d, 16, dir, &t->totalKernel, &t->totalMemory);
     t->data = P->buf[P->cur];
 }
 
@@ -1027,13 +1105,13 @@ void tope3DExecZ(struct topeFFT *f, struct topePlan3D *t)
 void tope3DUpload(struct topeFFT *f, struct topePlan3D *t, const double *d)
 {
     tope_impl *P = t ? impl_of(f, t->impl) : NULL;
-    if (P) impl_upload(f, P, d, &t->totalMemory);
+    if (P) impl_upload(f, P, d, 16, &t->totalMemory);
 }
 
 void tope3DDownload(struct topeFFT *f, struct topePlan3D *t, double *d)
 {
     tope_impl *P = t ? impl_of(f, t->impl) : NULL;
-    if (P) impl_download(f, P, d, &t->totalKernel, &t->totalMemory);
+    if (P) impl_download(f, P, d, 16, &t->totalKernel, &t->totalMemory);
 }
 
 void tope3DBitrevPermute(struct topeFFT *f, struct topePlan3D *t, int axis)

@@ -83,6 +83,7 @@ class TopePlan3D(C.Structure):
 _F = C.POINTER(TopeFFT)
 _P1, _P2, _P3 = C.POINTER(TopePlan1D), C.POINTER(TopePlan2D), C.POINTER(TopePlan3D)
 _D = C.POINTER(C.c_double)
+_FL = C.POINTER(C.c_float)
 
 # (name, restype, argtypes) of every exported entry point of include/topefft.h
 # and include/topefft_ext.h
@@ -129,6 +130,14 @@ SIGNATURES = [
     ("topeResetPassTimes", None, [_F, _vp]),
     ("topePassInfo", C.c_int, [_F, _vp, C.c_int, C.POINTER(C.c_int64)]),
     ("topeExec1DNoAlloc", C.c_int, [_vp, _vp, C.c_int, C.c_int, _vp]),
+    ("tope1DBatchPlanInitF32", None, [_F, _P1, C.c_int, C.c_int, C.c_int, _FL]),
+    ("tope2DPlanInitF32", None, [_F, _P2, C.c_int, C.c_int, C.c_int, _FL]),
+    ("tope3DPlanInitF32", None, [_F, _P3, C.c_int, C.c_int, C.c_int, C.c_int, _FL]),
+    ("tope1DExecF32", None, [_F, _P1, _FL, C.c_int]),
+    ("tope2DExecF32", None, [_F, _P2, _FL, C.c_int]),
+    ("tope3DExecF32", None, [_F, _P3, _FL, C.c_int]),
+    ("topeUploadF32", None, [_F, _vp, _FL]),
+    ("topeDownloadF32", None, [_F, _vp, _FL]),
 ]
 
 
@@ -271,6 +280,44 @@ def topeGetLastError() -> int:
 
 def topeErrorString(st: int) -> str:
     return lib.topeErrorString(st).decode()
+
+
+def _fptr(d):
+    if d is None:
+        return None
+    if isinstance(d, np.ndarray):
+        if d.dtype != np.float32 or not d.flags.c_contiguous:
+            raise TypeError("data must be a C-contiguous float32 array")
+        return d.ctypes.data_as(_FL)
+    if isinstance(d, int):
+        return C.cast(d, _FL)
+    raise TypeError("unsupported data argument")
+
+
+def tope1DBatchPlanInitF32(f, t, x, batch, type_, d) -> None:
+    lib.tope1DBatchPlanInitF32(C.byref(f), C.byref(t), x, batch, type_, _fptr(d))
+
+
+def tope2DPlanInitF32(f, t, x, y, type_, d) -> None:
+    lib.tope2DPlanInitF32(C.byref(f), C.byref(t), x, y, type_, _fptr(d))
+
+
+def tope3DPlanInitF32(f, t, x, y, z, type_, d) -> None:
+    lib.tope3DPlanInitF32(C.byref(f), C.byref(t), x, y, z, type_, _fptr(d))
+
+
+def execF32(f, t, d, dir_) -> None:
+    fn = {TopePlan1D: lib.tope1DExecF32, TopePlan2D: lib.tope2DExecF32,
+          TopePlan3D: lib.tope3DExecF32}[type(t)]
+    fn(C.byref(f), C.byref(t), _fptr(d), dir_)
+
+
+def uploadF32(f, t, d) -> None:
+    lib.topeUploadF32(C.byref(f), t.impl, _fptr(d))
+
+
+def downloadF32(f, t, d) -> None:
+    lib.topeDownloadF32(C.byref(f), t.impl, _fptr(d))
 
 
 def pass_times(f, t):
