@@ -304,6 +304,7 @@ def run_gpu(args, wl: dict) -> dict:
     T.topeFFTInit(f)
     T.check(f)
     T.topeSetArith(f, T.TOPE_ARITH_DF64 if args.arith == "df64" else T.TOPE_ARITH_FP64)
+    T.topeSetSplitMode(f, T.TOPE_SPLIT_FAST if args.split == "fast" else T.TOPE_SPLIT_ACCURATE)
 
     def make_plan(data, single):
         if ny * nz == 1:
@@ -400,7 +401,7 @@ def run_gpu(args, wl: dict) -> dict:
         ach = bytes_per_launch / avg_ns  # bytes/ns == GB/s
         roof = {"bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(ach / peak, 4), "peak_source": peak_kind,
-                "traffic": ncu_traffic(args.workload, "f32" if f32 else args.arith),
+                "traffic": ncu_traffic(args.workload, ("f32" if args.split == "fast" else "df32") if f32 else args.arith),
                 "kernel": f"pass_kernel L=2^{dom['log_l']} B={dom['b_tile']} "
                           f"({dom['ctas']} CTAs x {dom['threads']} threads)",
                 "launch_us": round(avg_ns / 1e3, 2),
@@ -440,9 +441,15 @@ def run_gpu(args, wl: dict) -> dict:
 
     destroy(t)
 
-    arith_desc = ("split precision: FP32 data and butterflies, FP64-accurate hi/lo twiddles"
-                  if f32 else "double-float (FP32 pairs) on FP64 storage" if args.arith == "df64"
-                  else "native FP64")
+    if f32 and args.split == "fast":
+        arith_desc = "split precision, fast: FP32 data and butterflies, FP64-accurate hi/lo twiddles"
+    elif f32:
+        arith_desc = ("split precision, accurate: FP32 data, double-float butterflies on chip, "
+                      "FP64-accurate hi/lo twiddles")
+    elif args.arith == "df64":
+        arith_desc = "double-float (FP32 pairs) on FP64 storage"
+    else:
+        arith_desc = "native FP64"
     res = {
         "metric": METRIC, "value": round(value_gflops, 3), "unit": "GFLOP/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
@@ -499,6 +506,8 @@ def main(argv=None):
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="1d_2p24")
     ap.add_argument("--arith", choices=["fp64", "df64"], default="fp64")
+    ap.add_argument("--split", choices=["accurate", "fast"], default="accurate",
+                    help="arithmetic of the FP32 (split-precision) workloads")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args(argv)
     if args.warmup < 3 and args.impl == "ours":

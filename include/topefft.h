@@ -139,6 +139,7 @@ struct topeFFT {
     int arith;                   /* TOPE_ARITH_* for plans made afterwards */
     int live_plans;
     int pass_timing;             /* per-launch timing on (topeSetPassTiming) */
+    int split_mode;              /* TOPE_SPLIT_* for FP32 plans made afterwards */
 };
 
 /* util.c:12 - elapsed nanoseconds of an event pair (f->event) */

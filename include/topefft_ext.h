@@ -76,11 +76,19 @@ void tope1DBatchPlanInit(struct topeFFT *f, struct topePlan1D *t, int x, int bat
 
 /* ---- split-precision form: FP32 complex data ----------------------------- */
 /* Same plans and semantics as the FP64 entry points, with interleaved FP32
- * complex data (half the memory traffic).  Arithmetic is FP32; twiddle
- * factors and the radix-16 constants are FP64-accurate (hi, lo) FP32 pairs,
- * generated from FP64 sincospi.  The FP64 Exec/Upload/Download entry
- * points reject these plans (and the F32 ones reject FP64 plans) with
- * TOPE_ERR_INVALID_ARG.  Device-resident execution uses tope*DExecDevice. */
+ * complex data (half the memory traffic).  Twiddle factors and the radix-16
+ * constants are FP64-accurate (hi, lo) FP32 pairs from FP64 sincospi.
+ * Two arithmetics, chosen by topeSetSplitMode before the plan is made:
+ *   TOPE_SPLIT_ACCURATE (default): double-float butterflies on chip, so only
+ *     the FP32 loads and stores round; rel-L2 <= 1e-7 against an FP64
+ *     transform of the unrounded input at 512^3;
+ *   TOPE_SPLIT_FAST: FP32 butterflies; about 1e-7 to 1.6e-7 rel-L2 at the
+ *     same sizes (an FP32 FFT's own rounding error, ~u*sqrt(log2 N)).
+ * The FP64 Exec/Upload/Download entry points reject these plans (and the
+ * F32 ones reject FP64 plans) with TOPE_ERR_INVALID_ARG.  Device-resident
+ * execution uses tope*DExecDevice. */
+enum topeSplitMode { TOPE_SPLIT_ACCURATE = 0, TOPE_SPLIT_FAST = 1 };
+void topeSetSplitMode(struct topeFFT *f, int mode);
 void tope1DBatchPlanInitF32(struct topeFFT *f, struct topePlan1D *t, int x, int batch, int type,
                             float *d);
 void tope2DPlanInitF32(struct topeFFT *f, struct topePlan2D *t, int x, int y, int type, float *d);

@@ -1,11 +1,13 @@
-"""GPU parity of the split-precision form (FP32 data, FP32 butterflies with
-FP64-accurate hi/lo twiddles), through the C interface.
+"""GPU parity of the split-precision form (FP32 data, FP64-accurate hi/lo
+twiddles), through the C interface, in both of its modes: accurate
+(double-float butterflies on chip) and fast (FP32 butterflies).
 
 Inputs follow the benchmark configuration of this form: the uniform[-1,1)
 field plus a Gaussian pulse of amplitude 1e6 (sigma = 4 samples per axis)
 added to the real part at the grid centre (per row for batched 1D), which
 stresses dynamic range.  The FP64 oracle runs on the FP64 values before
-they are rounded to FP32.  Gate: rel-L2 <= 1e-7; max-abs is reported.
+they are rounded to FP32.  Gate: rel-L2 <= 1e-7 (accurate mode); max-abs is
+reported.
 """
 import numpy as np
 import pytest
@@ -14,16 +16,22 @@ from conftest import SEED0
 
 pytestmark = pytest.mark.gpu
 
-GATE = 1e-7
+# the accurate mode (double-float butterflies, FP32 only in memory) meets
+# the benchmark gate; the fast mode (FP32 butterflies) carries an FP32 FFT's
+# own rounding error, measured 1.0e-7..1.6e-7 on these inputs
+GATES = {"accurate": 1e-7, "fast": 2.5e-7}
 
 
-@pytest.fixture
-def fw(T):
-    """FP32 plans ignore the framework's FP64-storage arithmetic setting, so
-    one framework per test (not one per arithmetic) is enough."""
+@pytest.fixture(params=["accurate", "fast"])
+def fw(T, request):
+    """One framework per split mode (FP32 plans ignore the FP64-storage
+    arithmetic setting)."""
     f = T.TopeFFT()
     T.topeFFTInit(f)
     T.check(f)
+    T.topeSetSplitMode(f, T.TOPE_SPLIT_FAST if request.param == "fast" else T.TOPE_SPLIT_ACCURATE)
+    T.check(f)
+    f.gate = GATES[request.param]
     yield f
     T.topeFFTDestroy(f)
 
@@ -81,7 +89,7 @@ def test_f32_error_vs_fp64_oracle(T, fw, orc, dims, batch):
         err_alg = orc.rel_l2(got, ref_r)
         print(f"{dims} x{batch} dir={dir_}: rel-L2 {err:.2e} (vs rounded input {err_alg:.2e}), "
               f"max-abs {orc.max_abs(got, ref):.3e}")
-        assert err <= GATE and err_alg <= GATE
+        assert err <= fw.gate and err_alg <= fw.gate
 
 
 @pytest.mark.parametrize("dims,batch", [((512, 512, 512), 1), ((1 << 14, 1, 1), 4096)],
@@ -94,7 +102,7 @@ def test_f32_full_size(T, fw, orc, dims, batch):
     ref = oracle_fp64(orc, x, dims, 1, batch)
     err = orc.rel_l2(got, ref)
     print(f"{dims} x{batch}: rel-L2 {err:.2e}, max-abs {orc.max_abs(got, ref):.3e}")
-    assert err <= GATE
+    assert err <= fw.gate
 
 
 def test_f32_round_trip_and_type_checks(T, fw, orc):

@@ -452,6 +452,34 @@ struct ArithDF64 {
 };
 
 /* ------------------------------------------------------------------------ */
+/* split precision, accurate: FP32 in memory, double-float on chip.  A load  */
+/* is exact (hi = x, lo = 0); a store rounds hi + lo once.  FP32 storage has */
+/* FP32's exponent range, so no tile scaling is needed.                      */
+/* ------------------------------------------------------------------------ */
+struct ArithDF32 : ArithDF64 {
+    using Store = float2;
+    static constexpr int kId = 3;
+    static constexpr bool kScaled = false;
+    static __host__ __device__ __forceinline__ C load_s(float2 v, int)
+    {
+        C c;
+        c.r = df2{v.x, 0.f};
+        c.i = df2{v.y, 0.f};
+        return c;
+    }
+    static __host__ __device__ __forceinline__ float2 store_s(C v, int, double scale)
+    {
+        float2 o = make_float2(add_rn(v.r.h, v.r.l), add_rn(v.i.h, v.i.l));
+        if (scale != 1.0) {
+            const float s = (float)scale; /* a power of two: exact */
+            o.x *= s;
+            o.y *= s;
+        }
+        return o;
+    }
+};
+
+/* ------------------------------------------------------------------------ */
 /* split precision: FP32 data, FP32 arithmetic, twiddles and the DFT-16      */
 /* constants carried as FP64-accurate (hi, lo) FP32 pairs, so every product */
 /* with an irrational factor has one rounding instead of two.               */

@@ -32,6 +32,14 @@ static LaunchFn find(int log_l, int b_tile, int arith)
         if (log_l <= 11) return launcher_df64_4(log_l, log_b);
         return launcher_df64_5(log_l, log_b);
     }
+    if (arith == TFFT_ARITH_DF32) {
+        if (log_l <= 4) return launcher_df32_0(log_l, log_b);
+        if (log_l <= 6) return launcher_df32_1(log_l, log_b);
+        if (log_l <= 8) return launcher_df32_2(log_l, log_b);
+        if (log_l <= 9) return launcher_df32_3(log_l, log_b);
+        if (log_l <= 11) return launcher_df32_4(log_l, log_b);
+        return launcher_df32_5(log_l, log_b);
+    }
     return nullptr;
 }
 

@@ -380,6 +380,12 @@ LaunchFn launcher_df64_4(int log_l, int log_b);
 LaunchFn launcher_df64_5(int log_l, int log_b);
 LaunchFn launcher_f32_lo(int log_l, int log_b);
 LaunchFn launcher_f32_hi(int log_l, int log_b);
+LaunchFn launcher_df32_0(int log_l, int log_b);
+LaunchFn launcher_df32_1(int log_l, int log_b);
+LaunchFn launcher_df32_2(int log_l, int log_b);
+LaunchFn launcher_df32_3(int log_l, int log_b);
+LaunchFn launcher_df32_4(int log_l, int log_b);
+LaunchFn launcher_df32_5(int log_l, int log_b);
 
 } // namespace tfft
 

@@ -16,15 +16,19 @@ enum tfft_arith {
     TFFT_ARITH_F64 = 0,  /* native double-precision instructions          */
     TFFT_ARITH_DF64 = 1, /* double-float: FP32 (hi, lo) pairs on the FP32
                             pipe; FP64 loads/stores and FP64-accurate tables */
-    TFFT_ARITH_F32 = 2,  /* split precision: FP32 storage and arithmetic,
-                            twiddles as FP64-accurate (hi, lo) FP32 pairs   */
+    TFFT_ARITH_F32 = 2,  /* split precision, fast: FP32 storage and FP32
+                            butterflies, twiddles as FP64-accurate (hi, lo)
+                            FP32 pairs                                        */
+    TFFT_ARITH_DF32 = 3, /* split precision, accurate: FP32 storage, double-
+                            float butterflies on chip, so only the FP32 loads
+                            and stores round                                  */
 };
 
 /* bytes of one complex element in memory for an arithmetic */
-#define TFFT_ELEM_BYTES(arith) ((arith) == TFFT_ARITH_F32 ? 8 : 16)
+#define TFFT_ELEM_BYTES(arith) ((arith) >= TFFT_ARITH_F32 ? 8 : 16)
 
 /* Largest line length one CTA transforms: 2^13 complex points for 16-byte
- * elements, 2^14 for FP32 complex. */
+ * on-chip elements, 2^14 for FP32 complex. */
 #define TFFT_MAX_LOG_L 14
 #define TFFT_MAX_LOG_L_ARITH(arith) ((arith) == TFFT_ARITH_F32 ? 14 : 13)
 

@@ -174,6 +174,22 @@ void topeSetArith(struct topeFFT *f, int arith)
     set_status(f, TOPE_SUCCESS);
 }
 
+void topeSetSplitMode(struct topeFFT *f, int mode)
+{
+    if (!f || (mode != TOPE_SPLIT_ACCURATE && mode != TOPE_SPLIT_FAST)) {
+        set_status(f, TOPE_ERR_INVALID_ARG);
+        return;
+    }
+    f->split_mode = mode;
+    set_status(f, TOPE_SUCCESS);
+}
+
+/* arithmetic of FP32 plans: double-float on chip unless the fast mode */
+static int split_arith(const struct topeFFT *f)
+{
+    return (f && f->split_mode == TOPE_SPLIT_FAST) ? TFFT_ARITH_F32 : TFFT_ARITH_DF32;
+}
+
 /* ------------------------------------------------------------------------ */
 /* plan                                                                     */
 /* ------------------------------------------------------------------------ */
@@ -826,7 +842,7 @@ void tope1DBatchPlanInit(struct topeFFT *f, struct topePlan1D *t, int x, int bat
 void tope1DBatchPlanInitF32(struct topeFFT *f, struct topePlan1D *t, int x, int batch, int type,
                             float *d)
 {
-    plan1d(f, t, x, batch, type, d, TFFT_ARITH_F32);
+    plan1d(f, t, x, batch, type, d, split_arith(f));
 }
 
 void tope1DExecF32(struct topeFFT *f, struct topePlan1D *t, float *d, int dir)
@@ -920,7 +936,7 @@ void tope2DPlanInit(struct topeFFT *f, struct topePlan2D *t, int x, int y, int t
 
 void tope2DPlanInitF32(struct topeFFT *f, struct topePlan2D *t, int x, int y, int type, float *d)
 {
-    plan2d(f, t, x, y, type, d, TFFT_ARITH_F32);
+    plan2d(f, t, x, y, type, d, split_arith(f));
 }
 
 void tope2DExecF32(struct topeFFT *f, struct topePlan2D *t, float *d, int dir)
@@ -1037,7 +1053,7 @@ void tope3DPlanInit(struct topeFFT *f, struct topePlan3D *t, int x, int y, int z
 void tope3DPlanInitF32(struct topeFFT *f, struct topePlan3D *t, int x, int y, int z, int type,
                        float *d)
 {
-    plan3d(f, t, x, y, z, type, d, TFFT_ARITH_F32);
+    plan3d(f, t, x, y, z, type, d, split_arith(f));
 }
 
 void tope3DExecF32(struct topeFFT *f, struct topePlan3D *t, float *d, int dir)

@@ -34,6 +34,7 @@ TOPE_ERR_DESTROYED = 6
 TOPE_ERR_UNSUPPORTED = 7
 TOPE_ERR_TIMEOUT = 8
 TOPE_ARITH_FP64, TOPE_ARITH_DF64 = 0, 1
+TOPE_SPLIT_ACCURATE, TOPE_SPLIT_FAST = 0, 1
 
 LIB_PATH = Path(__file__).resolve().parent / "libtopefft.so"
 
@@ -46,7 +47,7 @@ class TopeFFT(C.Structure):
                 ("program1D", _vp), ("program2D", _vp), ("program3D", _vp), ("context", _vp),
                 ("command_queue", _vp), ("ret_num_platforms", C.c_uint),
                 ("ret_num_devices", C.c_uint), ("device_ordinal", C.c_int), ("arith", C.c_int),
-                ("live_plans", C.c_int), ("pass_timing", C.c_int)]
+                ("live_plans", C.c_int), ("pass_timing", C.c_int), ("split_mode", C.c_int)]
 
 
 class TopePlan1D(C.Structure):
@@ -138,6 +139,7 @@ SIGNATURES = [
     ("tope3DExecF32", None, [_F, _P3, _FL, C.c_int]),
     ("topeUploadF32", None, [_F, _vp, _FL]),
     ("topeDownloadF32", None, [_F, _vp, _FL]),
+    ("topeSetSplitMode", None, [_F, C.c_int]),
 ]
 
 
@@ -178,6 +180,10 @@ def topeFFTDestroy(f: TopeFFT) -> None:
 
 def topeSetArith(f: TopeFFT, arith: int) -> None:
     lib.topeSetArith(C.byref(f), arith)
+
+
+def topeSetSplitMode(f: TopeFFT, mode: int) -> None:
+    lib.topeSetSplitMode(C.byref(f), mode)
 
 
 def topeSetPassTiming(f: TopeFFT, enable: int) -> None:
