@@ -60,7 +60,27 @@ WORKLOADS = {
                          "desc": "split precision: 1D C2C batched 4096 x 2^14, FP32 data, "
                                  "uniform field + Gaussian pulse 1e6 (sigma 4) per row, "
                                  "forward+inverse"},
+    "batch_uneven": {"uneven": True, "f32": False,
+                     "desc": "uneven batch: 20,000 1D transforms N=2^k, k~U{6..16}, plus 500 2D "
+                             "transforms with sides from {64..1024}, uniform re/im, FP64, "
+                             "forward+inverse; one persistent launch per direction from a "
+                             "captured CUDA graph"},
+    "batch_uneven_f32": {"uneven": True, "f32": True,
+                         "desc": "uneven batch as batch_uneven, split precision (FP32 data)"},
 }
+
+
+def uneven_shapes(seed=None, n1d=20000, n2d=500):
+    """The uneven batch: 1D lengths 2^k, k uniform on 6..16, then 2D shapes
+    with NX, NY drawn independently from {64,...,1024}; SplitMix64-seeded."""
+    u = splitmix_uniform((n1d + 2 * n2d + 1) // 2 + 1, SEED0 + 5 if seed is None else seed)
+    u01 = (u + 1.0) / 2.0
+    k = 6 + np.minimum((u01[:n1d] * 11).astype(int), 10)
+    sides = np.array([64, 128, 256, 512, 1024])
+    s = sides[np.minimum((u01[n1d:n1d + 2 * n2d] * 5).astype(int), 4)]
+    nx = [int(1 << int(v)) for v in k] + [int(v) for v in s[0::2]]
+    ny = [1] * n1d + [int(v) for v in s[1::2]]
+    return nx, ny
 METRIC = "C2C GFLOP/s & HBM GB/s vs roofline, FP64 plain vs split-precision at stated rel-L2"
 SEED0 = 0x70E0F0F7
 L2_BYTES = 129 * 10 ** 6
@@ -480,12 +500,176 @@ def run_gpu(args, wl: dict) -> dict:
     return res if rank == 0 else None
 
 
+def batch_flops(nx, ny) -> float:
+    return float(sum(2 * 5.0 * a * b * np.log2(a * b) for a, b in zip(nx, ny)))
+
+
+def batch_bytes_per_launch(nx, ny, es) -> int:
+    """algorithmic bytes of one direction: each pass reads and writes its
+    class once (1D up to 2^12 and ... one pass, longer 1D and 2D two)"""
+    tot = 0
+    for a, b in zip(nx, ny):
+        passes = 1 if (b == 1 and a <= 4096) else 2
+        tot += passes * 2 * es * a * b
+    return tot
+
+
+def run_batch(args, wl: dict) -> dict:
+    import torch
+    import __graft_entry__ as g
+    T = g.load_package()
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    os.environ["TOPEFFT_DEVICE"] = str(local)
+    dist = dist_init(ws, True)
+    f32 = wl["f32"]
+    es = 8 if f32 else 16
+    nx, ny = uneven_shapes()
+    total = sum(a * b for a, b in zip(nx, ny))
+    x = splitmix_uniform(total, SEED0 + 6)
+    xs = x.astype(np.float32) if f32 else x
+    del x
+    f = T.TopeFFT()
+    T.topeFFTInit(f)
+    T.check(f)
+    T.topeSetArith(f, T.TOPE_ARITH_DF64 if args.arith == "df64" else T.TOPE_ARITH_FP64)
+    T.topeSetSplitMode(f, T.TOPE_SPLIT_FAST if args.split == "fast" else T.TOPE_SPLIT_ACCURATE)
+    b = T.TopeBatch()
+    t_plan = time.perf_counter()
+    T.topeBatchPlanInit(f, b, nx, ny, T.C2C, xs)
+    t_plan = time.perf_counter() - t_plan
+    T.check(f)
+    stream = torch.cuda.ExternalStream(f.command_queue)
+    flops = batch_flops(nx, ny)
+
+    def timed(mode, steps, warm):
+        T.topeBatchSetMode(f, b, mode)
+        for _ in range(warm):
+            T.topeBatchExecDevice(f, b, T.FORWARD)
+            T.topeBatchExecDevice(f, b, T.INVERSE)
+        T.topeSync(f)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(steps):
+            T.topeBatchExecDevice(f, b, T.FORWARD)
+            T.topeBatchExecDevice(f, b, T.INVERSE)
+        e1.record(stream)
+        T.topeSync(f)
+        T.check(f)
+        return e0.elapsed_time(e1) / steps
+
+    sampler = ClockSampler(local)
+    sampler.start()
+    ms_local = timed(T.TOPE_BATCH_PERSISTENT, args.steps, args.warmup)
+    clocks = sampler.stop()
+    ms, value = aggregate(dist, ms_local, flops, device=torch.device("cuda", local))
+    ms_launches = timed(T.TOPE_BATCH_LAUNCHES, max(2, args.steps // 4), 1)
+    ms_loop = timed(T.TOPE_BATCH_LOOP, 2, 1)
+    T.topeBatchSetMode(f, b, T.TOPE_BATCH_PERSISTENT)
+    # accuracy: round trip of the last steps
+    back = np.empty_like(xs)
+    T.topeBatchDownload(f, b, back)
+    T.check(f)
+    x64 = xs.astype(np.float64)
+    rt = float(np.sqrt(np.sum((back.astype(np.float64) - x64) ** 2) / np.sum(x64 * x64)))
+    # e2e: upload from pinned memory, Exec forward and inverse with read-back
+    nbytes = xs.nbytes
+    hp = T.lib.topeHostAlloc(nbytes)
+    ctype = ctypes.c_float if f32 else ctypes.c_double
+    host = np.ctypeslib.as_array((ctype * xs.size).from_address(hp))
+    host[:] = xs
+    hbuf = host  # typed view for the Exec read-back
+    e2e_steps = max(2, min(args.steps, 5))
+    T.topeBatchUpload(f, b, hp)
+    T.topeBatchExec(f, b, hbuf, T.FORWARD)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        T.topeBatchUpload(f, b, hp)
+        T.topeBatchExec(f, b, hbuf, T.FORWARD)
+        T.topeBatchExec(f, b, hbuf, T.INVERSE)
+    t1 = time.perf_counter()
+    T.check(f)
+    e2e_ms, e2e_val = aggregate(dist, (t1 - t0) * 1e3 / e2e_steps, flops,
+                                device=torch.device("cuda", local))
+    T.lib.topeHostFree(hp)
+    classes, ctas, items = b.classes, b.ctas, b.work_items
+    T.topeBatchDestroy(f, b)
+    bytes_launch = batch_bytes_per_launch(nx, ny, es)
+    peak, peak_kind = measured_peaks()
+    ach = bytes_launch / (ms / 2 * 1e-3) / 1e9
+    res = {
+        "metric": METRIC, "value": round(value / 1e9, 3), "unit": "GFLOP/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32" if f32 else "f64", "data": "synthetic (SplitMix64-seeded)",
+        "config": {"workload": args.workload, "description": wl["desc"],
+                   "transforms": len(nx), "points": total, "classes": classes,
+                   "work_items": items, "persistent_ctas": ctas,
+                   "arith": ("split " + args.split) if f32 else args.arith,
+                   "l2": f"inputs larger than L2 ({total * es >> 20} MiB vs 129 MB L2)",
+                   "parallelism": f"replicas x{ws}"},
+        "modes_ms_per_step": {"persistent_graph": round(ms_local, 3),
+                              "per_class_launch_graph": round(ms_launches, 3),
+                              "per_transform_loop": round(ms_loop, 3)},
+        "speedup_vs_per_transform_loop": round(ms_loop / ms_local, 2),
+        "plan_seconds_incl_autotune": round(t_plan, 2),
+        "rel_l2_roundtrip": rt,
+        "roofline": {"bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(ach / peak, 4), "peak_source": peak_kind, "traffic": None,
+                     "kernel": "batch_kernel (one persistent launch per direction)",
+                     "bytes_per_launch": bytes_launch,
+                     "launch_us": round(ms / 2 * 1e3, 1)},
+        "e2e": {"value": round(e2e_val / 1e9, 3), "unit": "GFLOP/s",
+                "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": 2 * nbytes,
+                "ms_per_step": round(e2e_ms, 3)},
+        "gpu_launches": 2 * args.steps,
+        "clocks": clocks,
+    }
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        res["cpu_baseline"] = cpu_batch_rate(nx, ny)
+    if dist is not None:
+        dist.destroy_process_group()
+    return res if rank == 0 else None
+
+
+def cpu_batch_rate(nx, ny, budget_s=20.0):
+    """The reference's kernels on host cores over the first transforms of the
+    batch, one plan per transform (as the reference would run them)."""
+    import oracle
+    kind = "reference" if oracle.REF_SO.exists() else "port"
+    emu = oracle.RefEmu() if kind == "reference" else oracle.Oracle()
+    cores = os.cpu_count() or 1
+    emu.set_threads(cores)
+    flops, t, i = 0.0, 0.0, 0
+    while i < len(nx) and t < budget_s:
+        a, b = nx[i], ny[i]
+        xs = splitmix_uniform(a * b, SEED0 + i)
+        t0 = time.perf_counter()
+        y = emu.exec(xs, a, b, 1, 1)
+        emu.exec(y, a, b, 1, 0)
+        t += time.perf_counter() - t0
+        flops += 2 * 5.0 * a * b * np.log2(a * b)
+        i += 1
+    return {"value": round(flops / t / 1e9, 4), "unit": "GFLOP/s", "cores": cores, "kind": kind,
+            "sample": f"first {i} transforms of the batch, forward+inverse each, {t:.1f} s"}
+
+
 def run_reference(args, wl: dict):
     ws, rank, _ = dist_env()
     if rank != 0:
         return None
-    gflops, cpu = cpu_reference_rate(wl, budget_s=150.0 / max(1, args.steps + args.warmup) * args.steps,
-                                     steps=args.steps, warmup=min(args.warmup, 1))
+    if wl.get("uneven"):
+        nx, ny = uneven_shapes()
+        cpu = cpu_batch_rate(nx, ny, budget_s=60.0)
+        gflops = cpu["value"]
+        cpu["ms_per_step"] = batch_flops(nx, ny) / (gflops * 1e9) * 1e3
+    else:
+        gflops, cpu = cpu_reference_rate(
+            wl, budget_s=150.0 / max(1, args.steps + args.warmup) * args.steps,
+            steps=args.steps, warmup=min(args.warmup, 1))
     return {"impl": "reference", "metric": METRIC, "value": round(gflops, 4), "unit": "GFLOP/s",
             "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(cpu["ms_per_step"], 3), "higher_is_better": True,
@@ -513,7 +697,12 @@ def main(argv=None):
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
     wl = WORKLOADS[args.workload]
-    res = run_reference(args, wl) if args.impl == "reference" else run_gpu(args, wl)
+    if args.impl == "reference":
+        res = run_reference(args, wl)
+    elif wl.get("uneven"):
+        res = run_batch(args, wl)
+    else:
+        res = run_gpu(args, wl)
     if res is not None:
         print(json.dumps(res), flush=True)
 

@@ -101,6 +101,55 @@ void tope3DExecF32(struct topeFFT *f, struct topePlan3D *t, float *d, int dir);
 void topeUploadF32(struct topeFFT *f, void *impl, const float *d);
 void topeDownloadF32(struct topeFFT *f, void *impl, float *d);
 
+/* ---- batches of independent transforms of uneven sizes ------------------ */
+/* count transforms packed back to back in one buffer, transform i of
+ * nx[i] x ny[i] complex points (ny[i] == 1: a 1D transform of length
+ * nx[i]; else 2D, x fastest), all powers of two; 1D lengths up to 2^24,
+ * 2D sides up to 2^12.  The data stay in the caller's order; transforms of
+ * the same shape form a class, and every pass of every class becomes tiles
+ * of one work queue.  Execution modes (topeBatchSetMode):
+ *   TOPE_BATCH_PERSISTENT (default): one persistent launch over the whole
+ *     queue, replayed from a captured CUDA graph;
+ *   TOPE_BATCH_LAUNCHES: one launch per class and pass, captured in a graph;
+ *   TOPE_BATCH_LOOP: one launch sequence per transform, as a loop over
+ *     single-transform plans would do (the comparison baseline).
+ * The split of long 1D transforms into two passes and the persistent grid
+ * size are chosen by timing candidates at plan time (autotuning); results
+ * are cached per size in the file named by TOPEFFT_TUNE_CACHE (default
+ * $HOME/.cache/topefft_tune.txt; TOPEFFT_AUTOTUNE=0 disables tuning). */
+enum topeBatchMode { TOPE_BATCH_PERSISTENT = 0, TOPE_BATCH_LAUNCHES = 1, TOPE_BATCH_LOOP = 2 };
+
+struct topeBatch {
+    int count;              /* transforms */
+    int type;               /* C2C */
+    size_t dataSize;        /* bytes of the packed data */
+    uint64_t totalMemory;   /* ns: host<->device copies */
+    uint64_t totalPreKernel;/* ns: plan-time kernels (tables, tuning) */
+    uint64_t totalKernel;   /* ns: execute kernels */
+    void *data;             /* device copy of the packed data */
+    int mode;               /* TOPE_BATCH_* */
+    int elem_bytes;         /* 16 (FP64) or 8 (FP32) */
+    int classes;            /* distinct shapes */
+    int ctas;               /* persistent grid size chosen */
+    int64_t work_items;     /* tiles in the persistent queue */
+    void *impl;
+};
+
+void topeBatchPlanInit(struct topeFFT *f, struct topeBatch *b, int count, const int *nx,
+                       const int *ny, int type, double *d);
+void topeBatchPlanInitF32(struct topeFFT *f, struct topeBatch *b, int count, const int *nx,
+                          const int *ny, int type, float *d);
+/* transform the device copy and read it back into d (d may be NULL) */
+void topeBatchExec(struct topeFFT *f, struct topeBatch *b, double *d, int dir);
+void topeBatchExecF32(struct topeFFT *f, struct topeBatch *b, float *d, int dir);
+/* asynchronous, no read-back */
+void topeBatchExecDevice(struct topeFFT *f, struct topeBatch *b, int dir);
+/* synchronous copies of the packed data (elem_bytes per complex value) */
+void topeBatchUpload(struct topeFFT *f, struct topeBatch *b, const void *d);
+void topeBatchDownload(struct topeFFT *f, struct topeBatch *b, void *d);
+void topeBatchSetMode(struct topeFFT *f, struct topeBatch *b, int mode);
+void topeBatchDestroy(struct topeFFT *f, struct topeBatch *b);
+
 /* ---- tables and permutation (plan internals, exposed for inspection) ---- */
 /* Copy a device buffer to host memory (synchronous). */
 void topeCopyToHost(struct topeFFT *f, void *dst, const void *device_src, size_t bytes);

@@ -52,8 +52,9 @@ def test_headers_compile(tmp_path, compiler):
 
 def test_struct_layout_matches_mirror(T, tmp_path):
     structs = {"topeFFT": T.TopeFFT, "topePlan1D": T.TopePlan1D, "topePlan2D": T.TopePlan2D,
-               "topePlan3D": T.TopePlan3D}
-    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "topefft.h"', "int main(void){"]
+               "topePlan3D": T.TopePlan3D, "topeBatch": T.TopeBatch}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "topefft.h"',
+             '#include "topefft_ext.h"', "int main(void){"]
     for cname, py in structs.items():
         lines.append(f'printf("{cname} size %zu\\n", sizeof(struct {cname}));')
         for fname, _ in py._fields_:

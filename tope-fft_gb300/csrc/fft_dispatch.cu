@@ -54,6 +54,5 @@ extern "C" int tfft_launch_pass(const tfft_pass *p, void *stream)
 {
     tfft::LaunchFn f = tfft::find(p->log_l, p->b_tile, p->arith);
     if (!f) return (int)cudaErrorInvalidValue;
-    if (p->n[0] % p->b_tile) return (int)cudaErrorInvalidValue;
     return f(*p, (cudaStream_t)stream);
 }

@@ -229,30 +229,50 @@ __device__ __forceinline__ void fft_line_regs(typename A::C *a, typename A::S *s
     }
 }
 
-template <class A, int LOG_L, int B>
-__global__ void __launch_bounds__(Shape<LOG_L>::TPL * B)
-    pass_kernel(const tfft_pass p)
+/*
+ * One tile: lines tile*B .. tile*B+B-1 of the pass's g0 dimension (the last
+ * tile may be ragged: its missing lines compute on zeros and store nothing),
+ * for the g1/g2 coordinates encoded in tile.  L2ONLY selects loads that
+ * bypass L1 (ld.global.cg): needed when another CTA of the same launch
+ * wrote the data (the persistent batch kernel); a plain pass launch reads
+ * with the streaming hint.
+ */
+template <class A, int LOG_L, int B, bool L2ONLY>
+__device__ __forceinline__ void run_tile(const tfft_pass &p, int64_t tile, unsigned char *smem_raw)
 {
     using C = typename A::C;
     using SH = Shape<LOG_L>;
     constexpr int E = SH::E, TPL = SH::TPL;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
     typename A::S *sm = reinterpret_cast<typename A::S *>(smem_raw);
 
     const int tid = threadIdx.x;
     const int b = tid % B, j = tid / B;
-    const int64_t tiles0 = p.n[0] / B;
-    const int64_t blk = blockIdx.x;
-    const int64_t g0 = (blk % tiles0) * B + b;
-    const int64_t rest = blk / tiles0;
+    const int64_t tiles0 = (p.n[0] + B - 1) / B;
+    const int64_t g0 = (tile % tiles0) * B + b;
+    const int64_t rest = tile / tiles0;
     const int64_t g1 = rest % p.n[1], g2 = rest / p.n[1];
+    const bool live = g0 < p.n[0];
 
     using Store = typename A::Store;
-    const Store *in = reinterpret_cast<const Store *>(p.in) + g0 * p.is[0] + g1 * p.is[1] +
-                      g2 * p.is[2];
+    /* line bases from the stride or the per-line tables */
+    const int64_t t0 = p.tab0 && live ? __ldg(p.tab0 + g0) : -1;
+    const int64_t t1 = p.tab1 ? __ldg(p.tab1 + g1) : -1;
+    const int64_t ibase = (t0 >= 0 ? t0 : g0 * p.is[0]) + (t1 >= 0 ? t1 : g1 * p.is[1]) +
+                          g2 * p.is[2];
+    const int64_t obase = (t0 >= 0 ? t0 : g0 * p.os[0]) + (t1 >= 0 ? t1 : g1 * p.os[1]) +
+                          g2 * p.os[2];
+    const Store *in = reinterpret_cast<const Store *>(p.in) + ibase;
     Store raw[E];
 #pragma unroll
-    for (int q = 0; q < E; q++) raw[q] = __ldcs(in + (int64_t)(j + q * TPL) * p.ies);
+    for (int q = 0; q < E; q++) {
+        if (!live) {
+            raw[q] = Store{};
+        } else if constexpr (L2ONLY) {
+            raw[q] = __ldcg(in + (int64_t)(j + q * TPL) * p.ies);
+        } else {
+            raw[q] = __ldcs(in + (int64_t)(j + q * TPL) * p.ies);
+        }
+    }
     /* arithmetics with a narrower exponent range than their storage work on
      * the tile scaled by 2^-delta, delta = the tile's largest FP64 exponent */
     int delta = 0;
@@ -278,13 +298,22 @@ __global__ void __launch_bounds__(Shape<LOG_L>::TPL * B)
         }
     }
 
-    Store *out = reinterpret_cast<Store *>(p.out) + g0 * p.os[0] + g1 * p.os[1] +
-                 g2 * p.os[2];
+    Store *out = reinterpret_cast<Store *>(p.out) + obase;
+    if (live) {
 #pragma unroll
-    for (int q = 0; q < E; q++) {
-        C v = p.conj_out ? A::conj(a[q]) : a[q];
-        __stcs(out + (int64_t)(j + q * TPL) * p.oes, A::store_s(v, delta, p.scale));
+        for (int q = 0; q < E; q++) {
+            C v = p.conj_out ? A::conj(a[q]) : a[q];
+            __stcs(out + (int64_t)(j + q * TPL) * p.oes, A::store_s(v, delta, p.scale));
+        }
     }
+}
+
+template <class A, int LOG_L, int B>
+__global__ void __launch_bounds__(Shape<LOG_L>::TPL * B)
+    pass_kernel(const tfft_pass p)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    run_tile<A, LOG_L, B, false>(p, blockIdx.x, smem_raw);
 }
 
 template <class A, int LOG_L, int LOG_B>
@@ -305,7 +334,7 @@ int launch_pass(const tfft_pass &p, cudaStream_t s)
             attr_done |= bit;
         }
     }
-    const int64_t blocks = (p.n[0] / B) * p.n[1] * p.n[2];
+    const int64_t blocks = ((p.n[0] + B - 1) / B) * p.n[1] * p.n[2];
     if (blocks <= 0) return 0;
     kern<<<(unsigned)blocks, Shape<LOG_L>::TPL * B, smem, s>>>(p);
     return (int)cudaGetLastError();

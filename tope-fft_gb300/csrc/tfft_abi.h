@@ -64,7 +64,50 @@ typedef struct tfft_pass {
     int tw_shift;
     int64_t tw_n;
     const void *tw_hi, *tw_lo;
+    /* optional per-line base tables (device int64, in complex elements):
+     * when set, tab0[g0] replaces g0*is[0] (and g0*os[0]) and tab1[g1]
+     * replaces g1*is[1] (and g1*os[1]); used by batches of transforms that
+     * sit at arbitrary offsets of the caller's packed buffer */
+    const int64_t *tab0, *tab1;
 } tfft_pass;
+
+/* ---- batches of independent transforms (persistent kernel) --------------- */
+/* one pass over one class of same-shaped transforms */
+typedef struct tfft_bpass {
+    tfft_pass p;
+    int64_t tiles; /* work items of this pass */
+    int dep;       /* class-pass whose completion this one waits for, or -1 */
+    int extra;     /* tiles required of dep beyond its count (0; a test hook
+                      sets 1 to make the wait run out) */
+} tfft_bpass;
+
+/* one work item: tile `tile` of class-pass `cp` */
+typedef struct tfft_bitem {
+    int cp;
+    int pad;
+    int64_t tile;
+} tfft_bitem;
+
+/* lines per tile of the batch kernel for log2 L (256 threads per CTA) */
+#define TFFT_BATCH_THREADS 256
+#define TFFT_BATCH_MAX_LOG_L 12
+int tfft_batch_lines_per_tile(int log_l);
+/* CTAs of the persistent kernel that fit on the device at once */
+int tfft_batch_max_ctas(int arith, int *ctas);
+/* state: int32 [0] queue head, [1] error flag, [2 + i] tiles done of pass i;
+ * spin_limit bounds each dependency wait (iterations of ~100 ns) */
+int tfft_launch_batch(const tfft_bpass *d_passes, const tfft_bitem *d_items, int64_t n_items,
+                      int *d_state, int n_passes, int arith, int ctas, long long spin_limit,
+                      void *stream);
+/* capture "clear state + batch launch" on stream into an executable graph */
+int tfft_batch_graph(void **graph_exec, const tfft_bpass *d_passes, const tfft_bitem *d_items,
+                     int64_t n_items, int *d_state, int n_passes, int arith, int ctas,
+                     long long spin_limit, void *stream);
+int tfft_graph_launch(void *graph_exec, void *stream);
+int tfft_graph_destroy(void *graph_exec);
+/* capture a sequence of pass launches into an executable graph */
+int tfft_capture_begin(void *stream);
+int tfft_capture_end(void **graph_exec, void *stream);
 
 /* ---- device memory / streams / events (thin wrappers, return 0 or a
  *      CUDA error code) --------------------------------------------------- */

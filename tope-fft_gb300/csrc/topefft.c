@@ -21,6 +21,7 @@
 #include "../../include/topefft.h"
 #include "../../include/topefft_ext.h"
 #include "tfft_abi.h"
+#include "topefft_internal.h"
 
 #define TOPE_MAGIC 0x70EFF7u
 #define MAX_PASSES 12
@@ -1256,3 +1257,20 @@ void *topeHostAlloc(size_t bytes)
 }
 
 void topeHostFree(void *p) { tfft_host_free(p); }
+
+/* ------------------------------------------------------------------------ */
+/* helpers shared with batch.c (hidden: not part of the ABI)                */
+/* ------------------------------------------------------------------------ */
+TOPE_INTERNAL int tope_status(struct topeFFT *f, int st) { return set_status(f, st); }
+TOPE_INTERNAL int tope_cuda_status(struct topeFFT *f, int rc) { return cuda_status(f, rc); }
+TOPE_INTERNAL int tope_framework_ready(struct topeFFT *f)
+{
+    if (!f) return set_status(NULL, TOPE_ERR_INVALID_ARG);
+    return fw_of(f) ? TOPE_SUCCESS : fw_open(f);
+}
+TOPE_INTERNAL void tope_framework_plan_added(struct topeFFT *f) { f->live_plans++; }
+TOPE_INTERNAL void tope_framework_plan_removed(struct topeFFT *f)
+{
+    if (f->live_plans > 0) f->live_plans--;
+    if (f->live_plans == 0) fw_close(f);
+}

@@ -81,7 +81,18 @@ class TopePlan3D(C.Structure):
                 ("localSize", _vp), ("impl", _vp)]
 
 
+class TopeBatch(C.Structure):
+    _fields_ = [("count", C.c_int), ("type", C.c_int), ("dataSize", C.c_size_t),
+                ("totalMemory", _u64), ("totalPreKernel", _u64), ("totalKernel", _u64),
+                ("data", _vp), ("mode", C.c_int), ("elem_bytes", C.c_int), ("classes", C.c_int),
+                ("ctas", C.c_int), ("work_items", C.c_int64), ("impl", _vp)]
+
+
+TOPE_BATCH_PERSISTENT, TOPE_BATCH_LAUNCHES, TOPE_BATCH_LOOP = 0, 1, 2
+
 _F = C.POINTER(TopeFFT)
+_PB = C.POINTER(TopeBatch)
+_IP = C.POINTER(C.c_int)
 _P1, _P2, _P3 = C.POINTER(TopePlan1D), C.POINTER(TopePlan2D), C.POINTER(TopePlan3D)
 _D = C.POINTER(C.c_double)
 _FL = C.POINTER(C.c_float)
@@ -140,6 +151,15 @@ SIGNATURES = [
     ("topeUploadF32", None, [_F, _vp, _FL]),
     ("topeDownloadF32", None, [_F, _vp, _FL]),
     ("topeSetSplitMode", None, [_F, C.c_int]),
+    ("topeBatchPlanInit", None, [_F, _PB, C.c_int, _IP, _IP, C.c_int, _D]),
+    ("topeBatchPlanInitF32", None, [_F, _PB, C.c_int, _IP, _IP, C.c_int, _FL]),
+    ("topeBatchExec", None, [_F, _PB, _D, C.c_int]),
+    ("topeBatchExecF32", None, [_F, _PB, _FL, C.c_int]),
+    ("topeBatchExecDevice", None, [_F, _PB, C.c_int]),
+    ("topeBatchUpload", None, [_F, _PB, _vp]),
+    ("topeBatchDownload", None, [_F, _PB, _vp]),
+    ("topeBatchSetMode", None, [_F, _PB, C.c_int]),
+    ("topeBatchDestroy", None, [_F, _PB]),
 ]
 
 
@@ -324,6 +344,48 @@ def uploadF32(f, t, d) -> None:
 
 def downloadF32(f, t, d) -> None:
     lib.topeDownloadF32(C.byref(f), t.impl, _fptr(d))
+
+
+def _iarr(v):
+    a = np.ascontiguousarray(np.asarray(v, dtype=np.int32))
+    return a, a.ctypes.data_as(_IP)
+
+
+def topeBatchPlanInit(f, b, nx, ny, type_, d) -> None:
+    """nx, ny: sequences of per-transform sizes (ny[i] == 1 for 1D)."""
+    ax, px = _iarr(nx)
+    ay, py = _iarr(ny)
+    if np.asarray(d).dtype == np.float32:
+        lib.topeBatchPlanInitF32(C.byref(f), C.byref(b), len(ax), px, py, type_, _fptr(d))
+    else:
+        lib.topeBatchPlanInit(C.byref(f), C.byref(b), len(ax), px, py, type_, _ptr(d))
+
+
+def topeBatchExec(f, b, d, dir_) -> None:
+    if d is not None and np.asarray(d).dtype == np.float32:
+        lib.topeBatchExecF32(C.byref(f), C.byref(b), _fptr(d), dir_)
+    else:
+        lib.topeBatchExec(C.byref(f), C.byref(b), _ptr(d), dir_)
+
+
+def topeBatchExecDevice(f, b, dir_) -> None:
+    lib.topeBatchExecDevice(C.byref(f), C.byref(b), dir_)
+
+
+def topeBatchUpload(f, b, d) -> None:
+    lib.topeBatchUpload(C.byref(f), C.byref(b), d if isinstance(d, int) else d.ctypes.data)
+
+
+def topeBatchDownload(f, b, d) -> None:
+    lib.topeBatchDownload(C.byref(f), C.byref(b), d if isinstance(d, int) else d.ctypes.data)
+
+
+def topeBatchSetMode(f, b, mode) -> None:
+    lib.topeBatchSetMode(C.byref(f), C.byref(b), mode)
+
+
+def topeBatchDestroy(f, b) -> None:
+    lib.topeBatchDestroy(C.byref(f), C.byref(b))
 
 
 def pass_times(f, t):
