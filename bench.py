@@ -53,6 +53,12 @@ WORKLOADS = {
                "desc": "3D C2C FP64 256^3, forward+inverse, N(0,1) re/im"},
     "1d_4096": {"dims": (4096, 1, 1), "batch": 1,
                 "desc": "1D C2C FP64, N=4096, batch 1, forward+inverse, uniform[-1,1) re/im"},
+    "3d_512": {"dims": (512, 512, 512), "batch": 1,
+               "desc": "3D C2C FP64 512^3, forward+inverse, N(0,1) re/im (the FP64 comparison "
+                       "point of the split-precision 512^3 configuration)"},
+    "1d_4096x2p14": {"dims": (1 << 14, 1, 1), "batch": 4096,
+                     "desc": "1D C2C FP64 batched 4096 x 2^14, forward+inverse, uniform re/im "
+                             "(the FP64 comparison point of the split-precision configuration)"},
     "f32_3d_512": {"dims": (512, 512, 512), "batch": 1, "f32": True,
                    "desc": "split precision: 3D C2C 512^3, FP32 data, uniform[-1,1) field + "
                            "Gaussian pulse 1e6 (sigma 4) on the real part, forward+inverse"},
@@ -561,14 +567,18 @@ def run_batch(args, wl: dict) -> dict:
         T.check(f)
         return e0.elapsed_time(e1) / steps
 
+    auto_mode = b.mode  # chosen by the plan-time autotuner
     sampler = ClockSampler(local)
     sampler.start()
-    ms_local = timed(T.TOPE_BATCH_PERSISTENT, args.steps, args.warmup)
+    ms_local = timed(auto_mode, args.steps, args.warmup)
     clocks = sampler.stop()
     ms, value = aggregate(dist, ms_local, flops, device=torch.device("cuda", local))
-    ms_launches = timed(T.TOPE_BATCH_LAUNCHES, max(2, args.steps // 4), 1)
+    ms_persistent = (ms_local if auto_mode == T.TOPE_BATCH_PERSISTENT
+                     else timed(T.TOPE_BATCH_PERSISTENT, max(2, args.steps // 4), 1))
+    ms_launches = (ms_local if auto_mode == T.TOPE_BATCH_LAUNCHES
+                   else timed(T.TOPE_BATCH_LAUNCHES, max(2, args.steps // 4), 1))
     ms_loop = timed(T.TOPE_BATCH_LOOP, 2, 1)
-    T.topeBatchSetMode(f, b, T.TOPE_BATCH_PERSISTENT)
+    T.topeBatchSetMode(f, b, auto_mode)
     # accuracy: round trip of the last steps
     back = np.empty_like(xs)
     T.topeBatchDownload(f, b, back)
@@ -611,7 +621,8 @@ def run_batch(args, wl: dict) -> dict:
                    "arith": ("split " + args.split) if f32 else args.arith,
                    "l2": f"inputs larger than L2 ({total * es >> 20} MiB vs 129 MB L2)",
                    "parallelism": f"replicas x{ws}"},
-        "modes_ms_per_step": {"persistent_graph": round(ms_local, 3),
+        "mode": {0: "persistent_graph", 1: "per_class_launch_graph"}.get(auto_mode, "loop"),
+        "modes_ms_per_step": {"persistent_graph": round(ms_persistent, 3),
                               "per_class_launch_graph": round(ms_launches, 3),
                               "per_transform_loop": round(ms_loop, 3)},
         "speedup_vs_per_transform_loop": round(ms_loop / ms_local, 2),
@@ -619,7 +630,8 @@ def run_batch(args, wl: dict) -> dict:
         "rel_l2_roundtrip": rt,
         "roofline": {"bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(ach / peak, 4), "peak_source": peak_kind, "traffic": None,
-                     "kernel": "batch_kernel (one persistent launch per direction)",
+                     "kernel": ("batch_kernel (one persistent launch per direction)"
+                                if auto_mode == 0 else "pass_kernel launches (graph per direction)"),
                      "bytes_per_launch": bytes_launch,
                      "launch_us": round(ms / 2 * 1e3, 1)},
         "e2e": {"value": round(e2e_val / 1e9, 3), "unit": "GFLOP/s",

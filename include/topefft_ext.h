@@ -108,15 +108,17 @@ void topeDownloadF32(struct topeFFT *f, void *impl, float *d);
  * 2D sides up to 2^12.  The data stay in the caller's order; transforms of
  * the same shape form a class, and every pass of every class becomes tiles
  * of one work queue.  Execution modes (topeBatchSetMode):
- *   TOPE_BATCH_PERSISTENT (default): one persistent launch over the whole
- *     queue, replayed from a captured CUDA graph;
+ *   TOPE_BATCH_PERSISTENT: one persistent launch over the whole queue,
+ *     replayed from a captured CUDA graph;
  *   TOPE_BATCH_LAUNCHES: one launch per class and pass, captured in a graph;
  *   TOPE_BATCH_LOOP: one launch sequence per transform, as a loop over
  *     single-transform plans would do (the comparison baseline).
- * The split of long 1D transforms into two passes and the persistent grid
- * size are chosen by timing candidates at plan time (autotuning); results
- * are cached per size in the file named by TOPEFFT_TUNE_CACHE (default
- * $HOME/.cache/topefft_tune.txt; TOPEFFT_AUTOTUNE=0 disables tuning). */
+ * Autotuning at plan time times candidates on the plan's own buffers: the
+ * split of long 1D transforms into two passes (cached per size in the file
+ * named by TOPEFFT_TUNE_CACHE, default $HOME/.cache/topefft_tune.txt), the
+ * persistent grid size, and the mode (persistent unless the per-class
+ * launch graph is at least 5% faster; b->mode reports the choice).
+ * TOPEFFT_AUTOTUNE=0 disables tuning (persistent mode, balanced splits). */
 enum topeBatchMode { TOPE_BATCH_PERSISTENT = 0, TOPE_BATCH_LAUNCHES = 1, TOPE_BATCH_LOOP = 2 };
 
 struct topeBatch {

@@ -668,6 +668,25 @@ static void batch_init(struct topeFFT *f, struct topeBatch *b, int count, const 
         if (h < a) P->ctas = maxc / 2;
     }
     if ((st = build_graphs(f, P))) goto fail;
+    /* execution structure: the persistent launch unless the per-class
+     * launch graph measures at least 5% faster */
+    P->mode = TOPE_BATCH_PERSISTENT;
+    if (autotune_enabled() && !P->test_stall) {
+        unsigned long long tp = ~0ull, tl = ~0ull;
+        for (int m = 0; m < 2; m++) {
+            void *g = m == 0 ? P->graph[1] : P->lgraph[1];
+            if (tfft_graph_launch(g, stream)) continue;
+            tfft_event_record(P->ev[0], stream);
+            for (int r = 0; r < 2; r++) tfft_graph_launch(g, stream);
+            tfft_event_record(P->ev[1], stream);
+            if (tfft_stream_sync(stream)) continue;
+            uint64_t ns = 0;
+            tfft_event_elapsed_ns(P->ev[0], P->ev[1], &ns);
+            if (m == 0) tp = ns;
+            else tl = ns;
+        }
+        if (tl < tp && (double)tl < 0.95 * (double)tp) P->mode = TOPE_BATCH_LAUNCHES;
+    }
     tfft_event_record(P->ev[3], stream);
     /* upload the caller's data */
     if (d) rc = tfft_h2d(P->buf[0], d, bytes, stream);
@@ -685,7 +704,7 @@ static void batch_init(struct topeFFT *f, struct topeBatch *b, int count, const 
     b->classes = P->nclass;
     b->ctas = P->ctas;
     b->work_items = P->nitems;
-    b->mode = TOPE_BATCH_PERSISTENT;
+    b->mode = P->mode;
     b->impl = P;
     tope_framework_plan_added(f);
     tope_status(f, TOPE_SUCCESS);
