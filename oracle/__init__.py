@@ -80,6 +80,7 @@ class Oracle:
         L.oracle_fft_ld.argtypes = [_D, C.c_int64, C.c_int]
         L.oracle_fftnd_ld.argtypes = [_D, C.c_int, C.c_int, C.c_int, C.c_int]
         L.oracle_dft_ld.argtypes = [_D, _D, C.c_int, C.c_int]
+        L.oracle_bluestein_ld.argtypes = [_D, _D, C.c_int64, C.c_int]
         for n in ("oracle_rel_l2", "oracle_max_abs"):
             getattr(L, n).restype = C.c_double
             getattr(L, n).argtypes = [_D, _D, C.c_int64]
@@ -150,6 +151,11 @@ class Oracle:
     def dft_ld(self, d: np.ndarray, n: int, dir_: int = 1) -> np.ndarray:
         out = np.empty(2 * n)
         self.lib.oracle_dft_ld(_ptr(np.ascontiguousarray(d)), _ptr(out), n, dir_)
+        return out
+
+    def bluestein_ld(self, d: np.ndarray, n: int, dir_: int = 1) -> np.ndarray:
+        out = np.empty(2 * n)
+        self.lib.oracle_bluestein_ld(_ptr(np.ascontiguousarray(d)), _ptr(out), n, dir_)
         return out
 
     # metrics ------------------------------------------------------------------

@@ -445,6 +445,57 @@ void oracle_dft_ld(const double *d, double *out, int n, int dir)
     free(ti);
 }
 
+/* Long-double transform of any length n through Bluestein's identity
+ * jk = (j^2 + k^2 - (k-j)^2)/2: X[k] = c[k] sum_j (x[j] c[j]) conj(c[k-j]),
+ * c[k] = exp(-pi i k^2/n), evaluated as a cyclic convolution of power-of-two
+ * length m >= 2n-1 with the long-double FFT above.  Fast enough for lengths
+ * where the O(n^2) sum is not; checked against oracle_dft_ld in the tests. */
+void oracle_bluestein_ld(const double *d, double *out, int64_t n, int dir)
+{
+    int64_t m = 1;
+    while (m < 2 * n - 1) m <<= 1;
+    ld *tr = (ld *)malloc(sizeof(ld) * m), *ti = (ld *)malloc(sizeof(ld) * m);
+    ld *cr = (ld *)malloc(sizeof(ld) * n), *ci = (ld *)malloc(sizeof(ld) * n);
+    ld *ar = (ld *)calloc(m, sizeof(ld)), *ai = (ld *)calloc(m, sizeof(ld));
+    ld *br = (ld *)calloc(m, sizeof(ld)), *bi = (ld *)calloc(m, sizeof(ld));
+    ld pi = acosl(-1.0L);
+    ld_table(m, tr, ti);
+    for (int64_t k = 0; k < n; k++) {
+        /* k^2 mod 2n exactly: k < 2^31 */
+        uint64_t q = ((uint64_t)k * (uint64_t)k) % (uint64_t)(2 * n);
+        ld a = pi * ((ld)q / (ld)n);
+        cr[k] = cosl(a);
+        ci[k] = dir ? -sinl(a) : sinl(a); /* the inverse uses conj(c) */
+    }
+    for (int64_t k = 0; k < n; k++) {
+        ar[k] = (ld)d[2 * k] * cr[k] - (ld)d[2 * k + 1] * ci[k];
+        ai[k] = (ld)d[2 * k] * ci[k] + (ld)d[2 * k + 1] * cr[k];
+        br[k] = cr[k];
+        bi[k] = -ci[k];
+        if (k) {
+            br[m - k] = cr[k];
+            bi[m - k] = -ci[k];
+        }
+    }
+    fft_ld_line(ar, ai, m, tr, ti, 1);
+    fft_ld_line(br, bi, m, tr, ti, 1);
+    for (int64_t k = 0; k < m; k++) {
+        ld r = ar[k] * br[k] - ai[k] * bi[k];
+        ai[k] = ar[k] * bi[k] + ai[k] * br[k];
+        ar[k] = r;
+    }
+    fft_ld_line(ar, ai, m, tr, ti, 0);
+    ld s = (dir ? 1.0L : 1.0L / (ld)n) / (ld)m;
+    for (int64_t k = 0; k < n; k++) {
+        ld r = ar[k] * cr[k] - ai[k] * ci[k];
+        ld i = ar[k] * ci[k] + ai[k] * cr[k];
+        out[2 * k] = (double)(r * s);
+        out[2 * k + 1] = (double)(i * s);
+    }
+    free(tr); free(ti); free(cr); free(ci);
+    free(ar); free(ai); free(br); free(bi);
+}
+
 /* ------------------------------------------------------------------------ */
 double oracle_rel_l2(const double *a, const double *ref, int64_t nd)
 {

@@ -53,6 +53,8 @@ void oracle_fft_ld(double *d, int64_t n, int dir);
 void oracle_fftnd_ld(double *d, int nx, int ny, int nz, int dir);
 /* O(n^2), any n; out-of-place */
 void oracle_dft_ld(const double *d, double *out, int n, int dir);
+/* any n in O(n log n): Bluestein's chirp-z identity over long-double FFTs */
+void oracle_bluestein_ld(const double *d, double *out, int64_t n, int dir);
 
 /* ---- metrics ------------------------------------------------------------- */
 double oracle_rel_l2(const double *a, const double *ref, int64_t n_doubles);

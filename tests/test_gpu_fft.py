@@ -143,6 +143,35 @@ def test_1d_non_power_of_two(T, fw, orc, golden, n):
     assert orc.rel_l2(run1d(T, fw, x, n, 0), orc.dft_ld(x, n, 0)) <= tol
 
 
+@pytest.mark.parametrize("n", [127, 128, 129, 4095, 10007, 100000, 999983, 3 << 20])
+def test_1d_non_power_of_two_long(T, fw, orc, n):
+    """Lengths from 128 on that are not powers of two run as chirp-z
+    convolutions over power-of-two sub-transforms; compared with the
+    long-double chirp-z oracle (itself pinned to the O(n^2) sum) and, where
+    that is quick, with the O(n^2) long-double sum."""
+    x = orc.uniform(n, SEED0 + 7 * n)
+    tol = 1e-13 * np.log2(n)
+    for dir_ in (1, 0):
+        got = run1d(T, fw, x, n, dir_)
+        assert orc.rel_l2(got, orc.bluestein_ld(x, n, dir_)) <= tol
+        if n <= 4095:
+            assert orc.rel_l2(got, orc.dft_ld(x, n, dir_)) <= tol
+
+
+def test_1d_non_power_of_two_round_trip(T, fw, orc):
+    n = 1000003
+    x = orc.uniform(n, SEED0 + 8)
+    d = x.copy()
+    t = T.TopePlan1D()
+    T.tope1DPlanInit(fw, t, n, T.C2C, d)
+    T.tope1DExec(fw, t, d, T.FORWARD)
+    assert abs(np.dot(d, d) / n / np.dot(x, x) - 1) < 1e-12
+    T.tope1DExec(fw, t, d, T.INVERSE)
+    T.check(fw)
+    assert orc.rel_l2(d, x) <= 1e-13 * np.log2(n)
+    T.tope1DDestroy(fw, t)
+
+
 @pytest.mark.parametrize("n", [16, 4096, 1 << 16])
 def test_known_answers(T, fw, n):
     delta = np.zeros(2 * n)

@@ -152,3 +152,16 @@ def test_parseval_linearity_roundtrip(orc):
     Z = orc.exec(2.5 * x - y, n)
     assert orc.rel_l2(Z, 2.5 * X - orc.exec(y, n)) < 1e-15
     assert orc.rel_l2(orc.exec(X, n, dir_=0), x) < 1e-15
+
+
+@pytest.mark.parametrize("n", [3, 7, 100, 129, 1000, 4095])
+@pytest.mark.parametrize("dir_", [1, 0], ids=["fwd", "inv"])
+def test_bluestein_ld_matches_direct_sum(orc, n, dir_):
+    """The long-double chirp-z oracle (used for long non-power-of-two lines)
+    agrees with the O(n^2) long-double sum and, for powers of two, with the
+    long-double FFT."""
+    x = orc.uniform(n, 300 + n)
+    assert orc.rel_l2(orc.bluestein_ld(x, n, dir_), orc.dft_ld(x, n, dir_)) <= 5e-17
+    p = 1 << 11
+    y = orc.uniform(p, 301)
+    assert orc.rel_l2(orc.bluestein_ld(y, p, dir_), orc.fft_ld(y, p, dir_=dir_)) <= 5e-17

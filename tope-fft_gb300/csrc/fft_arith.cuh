@@ -184,24 +184,15 @@ __host__ __device__ __forceinline__ unsigned dexp(double v)
  */
 __host__ __device__ __forceinline__ void split_double(double v, int delta, float &hi, float &lo)
 {
-    unsigned long long b = d2ull(v);
-    int e = (int)((b >> 52) & 0x7ffu);
-    if (e == 0) {
-        /* FP64 subnormal: normalise the significand first */
-        const unsigned long long mant = b & 0xfffffffffffffull;
-        if (!mant) {
-            hi = 0.f;
-            lo = 0.f;
-            return;
-        }
-        const int sh = clz64(mant) - 11;
-        b = (b & 0x8000000000000000ull) | ((mant << sh) & 0xfffffffffffffull);
-        e = 1 - sh;
-    }
+    const unsigned long long b = d2ull(v);
+    const int e = (int)((b >> 52) & 0x7ffu);
     const unsigned hw = (unsigned)(b >> 32), lw = (unsigned)b;
     const int E = e - 1023 - delta;
     const unsigned sign = hw & 0x80000000u;
-    if (E < -100) {
+    /* zeros and FP64 subnormals: a tile that can hold a subnormal within
+     * 2^100 of its largest value is lifted by 2^600 before the split (see
+     * run_tile), so here they are always far below the tile's rounding level */
+    if (e == 0 || E < -100) {
         hi = 0.f;
         lo = 0.f;
         return;

@@ -180,6 +180,72 @@ __global__ void k_bitrev_permute(double2 *d, const int *__restrict__ rev, int lo
     }
 }
 
+/* ---- Bluestein (chirp-z) for lengths that are not powers of two --------- */
+__device__ __forceinline__ double2 cmul(double2 a, double2 b)
+{
+    return make_double2(fma(a.x, b.x, -(a.y * b.y)), fma(a.x, b.y, a.y * b.x));
+}
+
+/* c[k] = exp(-pi i k^2 / n): k^2 reduced mod 2n exactly, one rounding */
+__global__ void k_chirp(double2 *c, int64_t n)
+{
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        /* k < 2^31, so k*k fits in 64 bits */
+        const int64_t m = (int64_t)(((uint64_t)k * (uint64_t)k) % (uint64_t)(2 * n));
+        double s, co;
+        sincospi((double)m / (double)n, &s, &co);
+        c[k] = make_double2(co, -s);
+    }
+}
+
+/* b[k] = conj(c[|k|]) on the cyclic index range of length m (zero between) */
+__global__ void k_bluestein_b(double2 *b, const double2 *__restrict__ c, int64_t n, int64_t m)
+{
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < m;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        double2 v = make_double2(0.0, 0.0);
+        if (k < n) v = c[k];
+        else if (k > m - n) v = c[m - k];
+        b[k] = make_double2(v.x, -v.y);
+    }
+}
+
+/* w[k] = x[k] c[k] (x conjugated first for an inverse), zero-padded to m */
+__global__ void k_bluestein_pre(const double2 *__restrict__ x, const double2 *__restrict__ c,
+                                double2 *__restrict__ w, int64_t n, int64_t m, int conj_in)
+{
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < m;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        double2 v = make_double2(0.0, 0.0);
+        if (k < n) {
+            double2 a = x[k];
+            if (conj_in) a.y = -a.y;
+            v = cmul(a, c[k]);
+        }
+        w[k] = v;
+    }
+}
+
+__global__ void k_pointwise(double2 *__restrict__ w, const double2 *__restrict__ h, int64_t m)
+{
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < m;
+         k += (int64_t)gridDim.x * blockDim.x)
+        w[k] = cmul(w[k], h[k]);
+}
+
+/* x[k] = w[k] c[k], conjugated and scaled for an inverse */
+__global__ void k_bluestein_post(const double2 *__restrict__ w, const double2 *__restrict__ c,
+                                 double2 *__restrict__ x, int64_t n, int conj_out, double scale)
+{
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        double2 v = cmul(w[k], c[k]);
+        if (conj_out) v.y = -v.y;
+        x[k] = make_double2(v.x * scale, v.y * scale);
+    }
+}
+
 __global__ void k_n2(double2 *d, int dir)
 {
     if (threadIdx.x == 0 && blockIdx.x == 0) {
@@ -253,6 +319,36 @@ int tfft_launch_bitrev_permute(void *d, const int *rev, int log2n, int64_t es, i
     const int64_t total = (int64_t(1) << log2n) * n0 * n1;
     k_bitrev_permute<<<grid_for(total, 256), 256, 0, (cudaStream_t)s>>>((double2 *)d, rev, log2n,
                                                                        es, n0, s0, n1, s1);
+    return (int)cudaGetLastError();
+}
+
+int tfft_bluestein_tables(void *chirp, void *b, int64_t n, int64_t m, void *s)
+{
+    cudaStream_t st = (cudaStream_t)s;
+    k_chirp<<<grid_for(n, 256), 256, 0, st>>>((double2 *)chirp, n);
+    k_bluestein_b<<<grid_for(m, 256), 256, 0, st>>>((double2 *)b, (const double2 *)chirp, n, m);
+    return (int)cudaGetLastError();
+}
+
+int tfft_bluestein_pre(const void *x, const void *chirp, void *w, int64_t n, int64_t m,
+                       int conj_in, void *s)
+{
+    k_bluestein_pre<<<grid_for(m, 256), 256, 0, (cudaStream_t)s>>>(
+        (const double2 *)x, (const double2 *)chirp, (double2 *)w, n, m, conj_in);
+    return (int)cudaGetLastError();
+}
+
+int tfft_pointwise(void *w, const void *h, int64_t m, void *s)
+{
+    k_pointwise<<<grid_for(m, 256), 256, 0, (cudaStream_t)s>>>((double2 *)w, (const double2 *)h, m);
+    return (int)cudaGetLastError();
+}
+
+int tfft_bluestein_post(const void *w, const void *chirp, void *x, int64_t n, int conj_out,
+                        double scale, void *s)
+{
+    k_bluestein_post<<<grid_for(n, 256), 256, 0, (cudaStream_t)s>>>(
+        (const double2 *)w, (const double2 *)chirp, (double2 *)x, n, conj_out, scale);
     return (int)cudaGetLastError();
 }
 

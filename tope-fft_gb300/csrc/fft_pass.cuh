@@ -275,8 +275,22 @@ __device__ __forceinline__ void run_tile(const tfft_pass &p, int64_t tile, unsig
     }
     /* arithmetics with a narrower exponent range than their storage work on
      * the tile scaled by 2^-delta, delta = the tile's largest FP64 exponent */
-    int delta = 0;
-    if constexpr (A::kScaled) delta = (int)tile_max_exp<TPL * B>(raw) - 1023;
+    int delta = 0, delta_out = 0;
+    if constexpr (A::kScaled) {
+        delta = delta_out = (int)tile_max_exp<TPL * B>(raw) - 1023;
+        /* the split takes normal FP64 values only: a tile whose largest
+         * magnitude is below 2^-900 may hold subnormals that matter, so the
+         * whole tile (a CTA-uniform branch) is lifted by 2^600, exactly, and
+         * the store puts the factor back */
+        if (delta < -900) {
+#pragma unroll
+            for (int q = 0; q < E; q++) {
+                raw[q].x *= 0x1p600;
+                raw[q].y *= 0x1p600;
+            }
+            delta += 600;
+        }
+    }
     C a[E];
 #pragma unroll
     for (int q = 0; q < E; q++) {
@@ -303,13 +317,24 @@ __device__ __forceinline__ void run_tile(const tfft_pass &p, int64_t tile, unsig
 #pragma unroll
         for (int q = 0; q < E; q++) {
             C v = p.conj_out ? A::conj(a[q]) : a[q];
-            __stcs(out + (int64_t)(j + q * TPL) * p.oes, A::store_s(v, delta, p.scale));
+            __stcs(out + (int64_t)(j + q * TPL) * p.oes, A::store_s(v, delta_out, p.scale));
         }
     }
 }
 
+/* double-float on FP64 storage: at least 16 resident warps per SM (a CTA of
+ * W warps asks for 16/W CTAs per SM, which caps a thread at 128 registers);
+ * the other arithmetics measured best with the compiler's own choice */
+template <class A, int T>
+constexpr int pass_min_blocks()
+{
+    constexpr int W = (T + 31) / 32;
+    return !A::kScaled || W >= 16 ? 1 : 16 / W;
+}
+
 template <class A, int LOG_L, int B>
-__global__ void __launch_bounds__(Shape<LOG_L>::TPL * B)
+__global__ void
+__launch_bounds__(Shape<LOG_L>::TPL * B, pass_min_blocks<A, Shape<LOG_L>::TPL * B>())
     pass_kernel(const tfft_pass p)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];

@@ -160,6 +160,20 @@ int tfft_launch_bitrev_permute(void *data, const int *rev, int log2n, int64_t es
 /* two-point transform in place (the reference's N == 2 case) */
 int tfft_launch_n2(void *data, int dir, void *stream);
 
+/* Bluestein (chirp-z) pieces for a length n that is not a power of two,
+ * computed through cyclic convolutions of length m >= 2n-1 (FP64):
+ *   tables: chirp[k] = exp(-pi i k^2/n), k < n; b = conj(chirp) laid out
+ *           cyclically over m points (to be transformed by the caller);
+ *   pre:    w = x * chirp zero-padded to m (x conjugated when conj_in);
+ *   pointwise: w *= h (m points);
+ *   post:   x = w * chirp, conjugated when conj_out, times scale. */
+int tfft_bluestein_tables(void *chirp, void *b, int64_t n, int64_t m, void *stream);
+int tfft_bluestein_pre(const void *x, const void *chirp, void *w, int64_t n, int64_t m,
+                       int conj_in, void *stream);
+int tfft_pointwise(void *w, const void *h, int64_t m, void *stream);
+int tfft_bluestein_post(const void *w, const void *chirp, void *x, int64_t n, int conj_out,
+                        double scale, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -194,7 +194,11 @@ static int split_arith(const struct topeFFT *f)
 /* ------------------------------------------------------------------------ */
 /* plan                                                                     */
 /* ------------------------------------------------------------------------ */
-enum { MODE_FFT = 0, MODE_N2 = 1, MODE_DFT = 2 };
+enum { MODE_FFT = 0, MODE_N2 = 1, MODE_DFT = 2, MODE_BLUESTEIN = 3 };
+
+/* lengths that are not powers of two: the O(N^2) DFT below this, Bluestein
+ * (three power-of-two FFTs of length >= 2N-1) from it on */
+#define BLUESTEIN_MIN_N 128
 
 typedef struct tope_impl {
     unsigned magic;
@@ -218,6 +222,10 @@ typedef struct tope_impl {
     int *bitrev[3];
     void *quarter[3];
     void *dft_tab;
+    /* Bluestein: power-of-two sub-plan of length m, chirp and transformed kernel */
+    struct tope_impl *sub;
+    void *chirp, *bhat;
+    int64_t bl_m;
     tope_evpair kev, mev;
     int pending;         /* kev recorded by an async exec, not yet accounted */
     int last_dir;
@@ -445,6 +453,9 @@ static void impl_free(tope_impl *P)
         tfft_free(P->quarter[a]);
     }
     tfft_free(P->dft_tab);
+    tfft_free(P->chirp);
+    tfft_free(P->bhat);
+    impl_free(P->sub);
     tfft_free(P->buf[0]);
     tfft_free(P->buf[1]);
     tfft_event_destroy(P->kev.a);
@@ -493,6 +504,9 @@ static void pev_settle(tope_impl *P)
     P->pev_used = 0;
 }
 
+static int run_passes(struct topeFFT *f, tope_impl *P, int first, int count, int dir,
+                      double scale);
+
 /* Build the device state of a plan and upload d (complex elements of the
  * arithmetic's storage type; arith < 0 takes the framework's setting).
  * Returns a status. */
@@ -537,7 +551,8 @@ static int impl_create(struct topeFFT *f, tope_impl **out, int ndim, int64_t x, 
     int lgx = ilog2_exact64(x), lgy = ilog2_exact64(y), lgz = ilog2_exact64(z);
     const int fp64_io = P->es == 16;
     if (ndim == 1 && x == 2 && batch == 1 && fp64_io) P->mode = MODE_N2;
-    else if (ndim == 1 && lgx < 0) P->mode = (batch == 1 && fp64_io) ? MODE_DFT : -1;
+    else if (ndim == 1 && lgx < 0)
+        P->mode = !(batch == 1 && fp64_io) ? -1 : x < BLUESTEIN_MIN_N ? MODE_DFT : MODE_BLUESTEIN;
     else if (lgx < 0 || lgy < 0 || lgz < 0) P->mode = -1;
     else P->mode = MODE_FFT;
     if (P->mode < 0) {
@@ -580,6 +595,26 @@ static int impl_create(struct topeFFT *f, tope_impl **out, int ndim, int64_t x, 
         if (tfft_malloc(&P->buf[1], bytes) || tfft_malloc(&P->dft_tab, 16 * (size_t)x))
             st = set_status(f, TOPE_ERR_ALLOC);
         else if ((rc = tfft_dft_table(P->dft_tab, (int)x, stream)))
+            st = cuda_status(f, rc);
+    } else if (P->mode == MODE_BLUESTEIN) {
+        /* X[k] = c[k] sum_j (x[j] c[j]) conj(c[k-j]), c[k] = exp(-pi i k^2/N):
+         * a cyclic convolution of length M >= 2N-1 through a power-of-two
+         * sub-plan; the kernel conj(c) is transformed once here */
+        int64_t m = 1;
+        while (m < 2 * x - 1) m <<= 1;
+        P->bl_m = m;
+        uint64_t t0 = 0, t1 = 0;
+        st = impl_create(f, &P->sub, 1, m, 1, 1, 1, NULL, P->arith, &t0, &t1);
+        if (!st) {
+            f->live_plans--; /* the sub-plan lives and dies with this plan */
+            if (tfft_malloc(&P->chirp, 16 * (size_t)x) || tfft_malloc(&P->bhat, 16 * (size_t)m))
+                st = set_status(f, TOPE_ERR_ALLOC);
+        }
+        tope_impl *S = P->sub;
+        if (!st && (rc = tfft_bluestein_tables(P->chirp, S->buf[S->cur], x, m, stream)))
+            st = cuda_status(f, rc);
+        if (!st) st = run_passes(f, S, 0, S->npass, FORWARD, 1.0);
+        if (!st && (rc = tfft_d2d(P->bhat, S->buf[S->cur], 16 * (size_t)m, stream)))
             st = cuda_status(f, rc);
     } else if (P->mode == MODE_N2) {
         /* the two-point plan keeps the reference's one-bit reversal table */
@@ -634,6 +669,7 @@ static tope_impl *impl_of(struct topeFFT *f, void *impl)
 static void settle(tope_impl *P, uint64_t *t_kernel)
 {
     pev_settle(P);
+    if (P->sub) pev_settle(P->sub);
     if (P->pending) {
         uint64_t ns = 0;
         tfft_event_elapsed_ns(P->kev.a, P->kev.b, &ns);
@@ -689,6 +725,20 @@ static int impl_exec_async(struct topeFFT *f, tope_impl *P, int dir)
                              stream);
         if (rc) st = cuda_status(f, rc);
         else P->cur = 1 - P->cur;
+    } else if (P->mode == MODE_BLUESTEIN) {
+        /* an inverse runs as conj(F(conj x))/N around the same convolution */
+        tope_impl *S = P->sub;
+        const int inv = dir == INVERSE;
+        const int64_t n = P->c[0], m = P->bl_m;
+        if ((rc = tfft_bluestein_pre(P->buf[P->cur], P->chirp, S->buf[S->cur], n, m, inv, stream)))
+            st = cuda_status(f, rc);
+        if (!st) st = run_passes(f, S, 0, S->npass, FORWARD, 1.0);
+        if (!st && (rc = tfft_pointwise(S->buf[S->cur], P->bhat, m, stream)))
+            st = cuda_status(f, rc);
+        if (!st) st = run_passes(f, S, 0, S->npass, INVERSE, 1.0 / (double)m);
+        if (!st && (rc = tfft_bluestein_post(S->buf[S->cur], P->chirp, P->buf[P->cur], n, inv,
+                                             inv ? 1.0 / (double)n : 1.0, stream)))
+            st = cuda_status(f, rc);
     }
     tfft_event_record(P->kev.b, stream);
     tfft_event_record(w->pair.b, stream);
@@ -825,7 +875,9 @@ static void plan1d(struct topeFFT *f, struct topePlan1D *t, int x, int batch, in
     t->impl = P;
     t->dataSize = (size_t)P->total * P->es;
     t->bitrev = P->bitrev[0];
-    t->twiddle = P->mode == MODE_DFT ? P->dft_tab : P->quarter[0];
+    t->twiddle = P->mode == MODE_DFT         ? P->dft_tab
+                 : P->mode == MODE_BLUESTEIN ? P->chirp
+                                             : P->quarter[0];
     sync_fields_1d(t, P);
 }
 
