@@ -73,6 +73,9 @@ WORKLOADS = {
                              "captured CUDA graph"},
     "batch_uneven_f32": {"uneven": True, "f32": True,
                          "desc": "uneven batch as batch_uneven, split precision (FP32 data)"},
+    "batch_uneven_small": {"uneven": True, "f32": False, "n1d": 2000, "n2d": 50,
+                           "desc": "uneven batch drawn like batch_uneven with 2,000 1D and 50 2D "
+                                   "transforms (a profiling-size case, ~0.5 GB), FP64"},
 }
 
 
@@ -87,6 +90,9 @@ def uneven_shapes(seed=None, n1d=20000, n2d=500):
     nx = [int(1 << int(v)) for v in k] + [int(v) for v in s[0::2]]
     ny = [1] * n1d + [int(v) for v in s[1::2]]
     return nx, ny
+# split-precision modes: library constant name, and the arithmetic name of its profiles
+SPLIT_MODES = {"accurate": 0, "fast": 1, "tensor": 2}
+SPLIT_ARITH = {"accurate": "df32", "fast": "f32", "tensor": "tc"}
 METRIC = "C2C GFLOP/s & HBM GB/s vs roofline, FP64 plain vs split-precision at stated rel-L2"
 SEED0 = 0x70E0F0F7
 L2_BYTES = 129 * 10 ** 6
@@ -330,7 +336,7 @@ def run_gpu(args, wl: dict) -> dict:
     T.topeFFTInit(f)
     T.check(f)
     T.topeSetArith(f, T.TOPE_ARITH_DF64 if args.arith == "df64" else T.TOPE_ARITH_FP64)
-    T.topeSetSplitMode(f, T.TOPE_SPLIT_FAST if args.split == "fast" else T.TOPE_SPLIT_ACCURATE)
+    T.topeSetSplitMode(f, SPLIT_MODES[args.split])
 
     def make_plan(data, single):
         if ny * nz == 1:
@@ -427,7 +433,7 @@ def run_gpu(args, wl: dict) -> dict:
         ach = bytes_per_launch / avg_ns  # bytes/ns == GB/s
         roof = {"bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(ach / peak, 4), "peak_source": peak_kind,
-                "traffic": ncu_traffic(args.workload, ("f32" if args.split == "fast" else "df32") if f32 else args.arith),
+                "traffic": ncu_traffic(args.workload, SPLIT_ARITH[args.split] if f32 else args.arith),
                 "kernel": f"pass_kernel L=2^{dom['log_l']} B={dom['b_tile']} "
                           f"({dom['ctas']} CTAs x {dom['threads']} threads)",
                 "launch_us": round(avg_ns / 1e3, 2),
@@ -469,6 +475,9 @@ def run_gpu(args, wl: dict) -> dict:
 
     if f32 and args.split == "fast":
         arith_desc = "split precision, fast: FP32 data and butterflies, FP64-accurate hi/lo twiddles"
+    elif f32 and args.split == "tensor":
+        arith_desc = ("split precision, tensor: FP32 data, radix-16 stages as tcgen05 GEMMs on "
+                      "3-way BF16 splits with FP32 accumulation, FP64-accurate hi/lo twiddles")
     elif f32:
         arith_desc = ("split precision, accurate: FP32 data, double-float butterflies on chip, "
                       "FP64-accurate hi/lo twiddles")
@@ -530,7 +539,7 @@ def run_batch(args, wl: dict) -> dict:
     dist = dist_init(ws, True)
     f32 = wl["f32"]
     es = 8 if f32 else 16
-    nx, ny = uneven_shapes()
+    nx, ny = uneven_shapes(n1d=wl.get("n1d", 20000), n2d=wl.get("n2d", 500))
     total = sum(a * b for a, b in zip(nx, ny))
     x = splitmix_uniform(total, SEED0 + 6)
     xs = x.astype(np.float32) if f32 else x
@@ -539,7 +548,7 @@ def run_batch(args, wl: dict) -> dict:
     T.topeFFTInit(f)
     T.check(f)
     T.topeSetArith(f, T.TOPE_ARITH_DF64 if args.arith == "df64" else T.TOPE_ARITH_FP64)
-    T.topeSetSplitMode(f, T.TOPE_SPLIT_FAST if args.split == "fast" else T.TOPE_SPLIT_ACCURATE)
+    T.topeSetSplitMode(f, SPLIT_MODES[args.split])
     b = T.TopeBatch()
     t_plan = time.perf_counter()
     T.topeBatchPlanInit(f, b, nx, ny, T.C2C, xs)
@@ -674,7 +683,7 @@ def run_reference(args, wl: dict):
     if rank != 0:
         return None
     if wl.get("uneven"):
-        nx, ny = uneven_shapes()
+        nx, ny = uneven_shapes(n1d=wl.get("n1d", 20000), n2d=wl.get("n2d", 500))
         cpu = cpu_batch_rate(nx, ny, budget_s=60.0)
         gflops = cpu["value"]
         cpu["ms_per_step"] = batch_flops(nx, ny) / (gflops * 1e9) * 1e3
@@ -702,7 +711,7 @@ def main(argv=None):
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="1d_2p24")
     ap.add_argument("--arith", choices=["fp64", "df64"], default="fp64")
-    ap.add_argument("--split", choices=["accurate", "fast"], default="accurate",
+    ap.add_argument("--split", choices=sorted(SPLIT_MODES), default="accurate",
                     help="arithmetic of the FP32 (split-precision) workloads")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args(argv)

@@ -74,6 +74,24 @@ void topeSync(struct topeFFT *f);
 void tope1DBatchPlanInit(struct topeFFT *f, struct topePlan1D *t, int x, int batch, int type,
                          double *d);
 
+/* ---- real data: type R2C ------------------------------------------------- */
+/* topefft.h defines R2C (src/topefft.h:9) but the reference implements only
+ * C2C; here tope1DPlanInit / tope1DBatchPlanInit with type R2C and an even
+ * length x make a real-data plan (FP64 storage, either arithmetic):
+ *   - PlanInit and tope1DUpload take x real doubles per row (row b at d + b*x);
+ *   - Exec(FORWARD) transforms the rows and writes the x/2 + 1 non-redundant
+ *     outputs X[0..x/2] of each row (e^{-2 pi i jk/x}, unnormalised) as
+ *     interleaved complex, row b at d + b*(x + 2): d must hold (x + 2)*batch
+ *     doubles;
+ *   - Exec(INVERSE) takes that spectrum (the device-resident one, or one
+ *     given to tope1DUploadSpectrum) and writes the x real values per row,
+ *     scaled by 1/x, so forward then inverse is a round trip;
+ *   - tope1DDownload returns the current data: the spectrum after a forward
+ *     transform, the real rows otherwise.
+ * The complex work is a transform of length x/2 on the packed reals
+ * (x[2j] + i x[2j+1]) plus one pre/post pass with W_x^k twiddles. */
+void tope1DUploadSpectrum(struct topeFFT *f, struct topePlan1D *t, const double *spec);
+
 /* ---- split-precision form: FP32 complex data ----------------------------- */
 /* Same plans and semantics as the FP64 entry points, with interleaved FP32
  * complex data (half the memory traffic).  Twiddle factors and the radix-16
@@ -83,11 +101,17 @@ void tope1DBatchPlanInit(struct topeFFT *f, struct topePlan1D *t, int x, int bat
  *     the FP32 loads and stores round; rel-L2 <= 1e-7 against an FP64
  *     transform of the unrounded input at 512^3;
  *   TOPE_SPLIT_FAST: FP32 butterflies; about 1e-7 to 1.6e-7 rel-L2 at the
- *     same sizes (an FP32 FFT's own rounding error, ~u*sqrt(log2 N)).
+ *     same sizes (an FP32 FFT's own rounding error, ~u*sqrt(log2 N));
+ *   TOPE_SPLIT_TENSOR: the radix-16 stages as tensor-core GEMMs on 3-way
+ *     BF16 splits with FP32 accumulation (lines up to 2^13 per pass, longer
+ *     ones in two passes); FP32-level error like TOPE_SPLIT_FAST.  Single
+ *     plans only: topeBatchPlanInitF32 rejects it with TOPE_ERR_UNSUPPORTED.
+ *     A wait for the tensor cores that gives up is reported by the
+ *     synchronous Exec as TOPE_ERR_TIMEOUT.
  * The FP64 Exec/Upload/Download entry points reject these plans (and the
  * F32 ones reject FP64 plans) with TOPE_ERR_INVALID_ARG.  Device-resident
  * execution uses tope*DExecDevice. */
-enum topeSplitMode { TOPE_SPLIT_ACCURATE = 0, TOPE_SPLIT_FAST = 1 };
+enum topeSplitMode { TOPE_SPLIT_ACCURATE = 0, TOPE_SPLIT_FAST = 1, TOPE_SPLIT_TENSOR = 2 };
 void topeSetSplitMode(struct topeFFT *f, int mode);
 void tope1DBatchPlanInitF32(struct topeFFT *f, struct topePlan1D *t, int x, int batch, int type,
                             float *d);

@@ -1,6 +1,7 @@
 """GPU parity of the split-precision form (FP32 data, FP64-accurate hi/lo
-twiddles), through the C interface, in both of its modes: accurate
-(double-float butterflies on chip) and fast (FP32 butterflies).
+twiddles), through the C interface, in its three modes: accurate
+(double-float butterflies on chip), fast (FP32 butterflies) and tensor (the
+radix-16 stages as tcgen05 GEMMs on 3-way BF16 splits).
 
 Inputs follow the benchmark configuration of this form: the uniform[-1,1)
 field plus a Gaussian pulse of amplitude 1e6 (sigma = 4 samples per axis)
@@ -18,18 +19,21 @@ pytestmark = pytest.mark.gpu
 
 # the accurate mode (double-float butterflies, FP32 only in memory) meets
 # the benchmark gate; the fast mode (FP32 butterflies) carries an FP32 FFT's
-# own rounding error, measured 1.0e-7..1.6e-7 on these inputs
-GATES = {"accurate": 1e-7, "fast": 2.5e-7}
+# own rounding error, measured 1.0e-7..1.6e-7 on these inputs; the tensor
+# mode (tcgen05 GEMMs on 3-way BF16 splits, FP32 accumulation in the tensor
+# cores) measured 1.7e-7..4.4e-7 (512^3)
+GATES = {"accurate": 1e-7, "fast": 2.5e-7, "tensor": 5e-7}
+MODES = {"accurate": 0, "fast": 1, "tensor": 2}
 
 
-@pytest.fixture(params=["accurate", "fast"])
+@pytest.fixture(params=["accurate", "fast", "tensor"])
 def fw(T, request):
     """One framework per split mode (FP32 plans ignore the FP64-storage
     arithmetic setting)."""
     f = T.TopeFFT()
     T.topeFFTInit(f)
     T.check(f)
-    T.topeSetSplitMode(f, T.TOPE_SPLIT_FAST if request.param == "fast" else T.TOPE_SPLIT_ACCURATE)
+    T.topeSetSplitMode(f, MODES[request.param])
     T.check(f)
     f.gate = GATES[request.param]
     yield f
@@ -120,3 +124,36 @@ def test_f32_round_trip_and_type_checks(T, fw, orc):
     assert fw.error == T.TOPE_ERR_INVALID_ARG
     T.tope1DDestroy(fw, t)
     T.check(fw)
+
+
+@pytest.mark.parametrize("lg,batch", [(4, 256), (4, 3), (5, 100), (8, 16), (9, 5), (12, 1),
+                                      (12, 3), (13, 2), (14, 2), (2, 8)])
+def test_tensor_mode_shapes(T, orc, lg, batch):
+    """Every line length of the tensor form (one row group per 128 16-point
+    sub-transforms, ragged last tiles, the four-step split above 2^13, the
+    FP32 kernel below 16 points) against the FP64 oracle."""
+    f = T.TopeFFT()
+    T.topeFFTInit(f)
+    T.topeSetSplitMode(f, T.TOPE_SPLIT_TENSOR)
+    T.check(f)
+    n = 1 << lg
+    x32 = orc.uniform(n * batch, SEED0 + lg).astype(np.float32)
+    for dir_ in (1, 0):
+        got = run_f32(T, f, x32, (n, 1, 1), dir_, batch).astype(np.float64)
+        ref = orc.exec(x32.astype(np.float64), n, 1, 1, dir_, batch=batch)
+        err = orc.rel_l2(got, ref)
+        print(f"tensor L=2^{lg} x{batch} dir={dir_}: rel-L2 {err:.2e}")
+        # measured 6e-8 (one stage) to 2.1e-7 (three stages, 2^12..2^13)
+        assert err <= 3e-7
+    T.topeFFTDestroy(f)
+
+
+def test_tensor_mode_rejected_by_batches(T):
+    f = T.TopeFFT()
+    T.topeFFTInit(f)
+    T.topeSetSplitMode(f, T.TOPE_SPLIT_TENSOR)
+    b = T.TopeBatch()
+    d = np.zeros(2 * 64, dtype=np.float32)
+    T.topeBatchPlanInit(f, b, [64], [1], T.C2C, d)
+    assert f.error == T.TOPE_ERR_UNSUPPORTED and not b.impl
+    T.topeFFTDestroy(f)

@@ -729,6 +729,12 @@ void topeBatchPlanInit(struct topeFFT *f, struct topeBatch *b, int count, const 
 void topeBatchPlanInitF32(struct topeFFT *f, struct topeBatch *b, int count, const int *nx,
                           const int *ny, int type, float *d)
 {
+    if (f && f->split_mode == TOPE_SPLIT_TENSOR) {
+        /* the persistent kernel has no tensor-core stages */
+        if (b) b->impl = NULL;
+        tope_status(f, TOPE_ERR_UNSUPPORTED);
+        return;
+    }
     int arith = (f && f->split_mode == TOPE_SPLIT_FAST) ? TFFT_ARITH_F32 : TFFT_ARITH_DF32;
     batch_init(f, b, count, nx, ny, type, d, arith);
 }

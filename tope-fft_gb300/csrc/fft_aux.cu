@@ -246,6 +246,67 @@ __global__ void k_bluestein_post(const double2 *__restrict__ w, const double2 *_
     }
 }
 
+/* real-data transforms of length n = 2m through a complex transform of
+ * length m: lo[i] = W_n^i (i < 2^shift), hi[h] = W_n^(h << shift) (h <= m >> shift),
+ * angles from the exact ratio (i mod n)/n, one rounding each */
+__global__ void k_real_tables(double2 *hi, double2 *lo, int64_t n, int shift, int64_t nhi)
+{
+    const int64_t nlo = int64_t(1) << shift;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nlo + nhi;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t e = i < nlo ? i : (i - nlo) << shift;
+        double s, c;
+        sincospi(2.0 * (double)(e % n) / (double)n, &s, &c);
+        if (i < nlo) lo[i] = make_double2(c, -s);
+        else hi[i - nlo] = make_double2(c, -s);
+    }
+}
+
+__device__ __forceinline__ double2 w_real(const double2 *hi, const double2 *lo, int shift, int64_t k)
+{
+    return cmul(hi[k >> shift], lo[k & ((int64_t(1) << shift) - 1)]);
+}
+
+/* forward: Z = FFT_m(x[2j] + i x[2j+1]) per row -> X[k], k = 0..m, with
+ * E = (Z[k] + conj Z[m-k])/2, O = (Z[k] - conj Z[m-k])/(2i), X = E + W_n^k O */
+__global__ void k_r2c_post(const double2 *__restrict__ z, double2 *__restrict__ x,
+                           const double2 *__restrict__ hi, const double2 *__restrict__ lo, int shift,
+                           int64_t m, int64_t rows)
+{
+    const int64_t per = m + 1;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < per * rows;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = i / per, k = i - r * per;
+        const double2 a = z[r * m + (k == m ? 0 : k)];
+        double2 b = z[r * m + (k == 0 ? 0 : m - k)];
+        b.y = -b.y;
+        const double2 e = make_double2(0.5 * (a.x + b.x), 0.5 * (a.y + b.y));
+        const double2 o = make_double2(0.5 * (a.y - b.y), -0.5 * (a.x - b.x));
+        const double2 wo = cmul(w_real(hi, lo, shift, k), o);
+        x[i] = make_double2(e.x + wo.x, e.y + wo.y);
+    }
+}
+
+/* inverse: X[0..m] per row -> Z[k] = E + i O, k < m, with E = (X[k] + conj X[m-k])/2,
+ * O = (X[k] - conj X[m-k]) conj(W_n^k) / 2; FFT_m^-1(Z) then holds x[2j] + i x[2j+1] */
+__global__ void k_c2r_pre(const double2 *__restrict__ x, double2 *__restrict__ z,
+                          const double2 *__restrict__ hi, const double2 *__restrict__ lo, int shift,
+                          int64_t m, int64_t rows)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m * rows;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = i / m, k = i - r * m;
+        const double2 a = x[r * (m + 1) + k];
+        double2 b = x[r * (m + 1) + m - k];
+        b.y = -b.y;
+        const double2 e = make_double2(0.5 * (a.x + b.x), 0.5 * (a.y + b.y));
+        double2 w = w_real(hi, lo, shift, k);
+        w.y = -w.y;
+        const double2 o = cmul(make_double2(0.5 * (a.x - b.x), 0.5 * (a.y - b.y)), w);
+        z[i] = make_double2(e.x - o.y, e.y + o.x);
+    }
+}
+
 __global__ void k_n2(double2 *d, int dir)
 {
     if (threadIdx.x == 0 && blockIdx.x == 0) {
@@ -349,6 +410,30 @@ int tfft_bluestein_post(const void *w, const void *chirp, void *x, int64_t n, in
 {
     k_bluestein_post<<<grid_for(n, 256), 256, 0, (cudaStream_t)s>>>(
         (const double2 *)w, (const double2 *)chirp, (double2 *)x, n, conj_out, scale);
+    return (int)cudaGetLastError();
+}
+
+int tfft_real_tables(void *hi, void *lo, int64_t n, int shift, void *s)
+{
+    const int64_t nhi = ((n / 2) >> shift) + 1;
+    k_real_tables<<<grid_for((int64_t(1) << shift) + nhi, 256), 256, 0, (cudaStream_t)s>>>(
+        (double2 *)hi, (double2 *)lo, n, shift, nhi);
+    return (int)cudaGetLastError();
+}
+
+int tfft_r2c_post(const void *z, void *x, const void *hi, const void *lo, int shift, int64_t m,
+                  int64_t rows, void *s)
+{
+    k_r2c_post<<<grid_for((m + 1) * rows, 256), 256, 0, (cudaStream_t)s>>>(
+        (const double2 *)z, (double2 *)x, (const double2 *)hi, (const double2 *)lo, shift, m, rows);
+    return (int)cudaGetLastError();
+}
+
+int tfft_c2r_pre(const void *x, void *z, const void *hi, const void *lo, int shift, int64_t m,
+                 int64_t rows, void *s)
+{
+    k_c2r_pre<<<grid_for(m * rows, 256), 256, 0, (cudaStream_t)s>>>(
+        (const double2 *)x, (double2 *)z, (const double2 *)hi, (const double2 *)lo, shift, m, rows);
     return (int)cudaGetLastError();
 }
 

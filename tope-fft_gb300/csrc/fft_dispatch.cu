@@ -18,11 +18,14 @@ static int ilog2_exact(int v)
 static LaunchFn find(int log_l, int b_tile, int arith)
 {
     const int log_b = ilog2_exact(b_tile);
+    /* the tensor form fixes its lines per CTA (up to 256 for L = 16) */
+    if (arith == TFFT_ARITH_TC && log_l >= 4)
+        return log_l <= 13 && b_tile == tfft_tc_b_tile(log_l) ? launcher_tc(log_l) : nullptr;
     if (log_l < 0 || log_l > TFFT_MAX_LOG_L || log_b < 0 || log_b > kMaxLogB) return nullptr;
     if (log_l > TFFT_MAX_LOG_L_ARITH(arith)) return nullptr;
     if (arith == TFFT_ARITH_F64)
         return log_l <= 9 ? launcher_f64_lo(log_l, log_b) : launcher_f64_hi(log_l, log_b);
-    if (arith == TFFT_ARITH_F32)
+    if (arith == TFFT_ARITH_F32 || (arith == TFFT_ARITH_TC && log_l < 4))
         return log_l <= 9 ? launcher_f32_lo(log_l, log_b) : launcher_f32_hi(log_l, log_b);
     if (arith == TFFT_ARITH_DF64) {
         if (log_l <= 4) return launcher_df64_0(log_l, log_b);

@@ -229,16 +229,29 @@ __device__ __forceinline__ void fft_line_regs(typename A::C *a, typename A::S *s
     }
 }
 
+/* the in-register line transform of run_tile: all stages on the CUDA cores */
+struct CoreLine {
+    template <class A, int LOG_L, int B>
+    __device__ __forceinline__ void run(typename A::C *a, typename A::S *sm, int j, int b,
+                                        const tfft_pass &p)
+    {
+        fft_line_regs<A, LOG_L, B>(a, sm, j, b, p.tw);
+    }
+};
+
 /*
  * One tile: lines tile*B .. tile*B+B-1 of the pass's g0 dimension (the last
- * tile may be ragged: its missing lines compute on zeros and store nothing),
+ * tile may be ragged: its missing lines compute on a copy of the last line
+ * and store nothing),
  * for the g1/g2 coordinates encoded in tile.  L2ONLY selects loads that
  * bypass L1 (ld.global.cg): needed when another CTA of the same launch
  * wrote the data (the persistent batch kernel); a plain pass launch reads
- * with the streaming hint.
+ * with the streaming hint.  LINE transforms the loaded points (CoreLine, or
+ * the tensor-core stages of fft_tc.cuh).
  */
-template <class A, int LOG_L, int B, bool L2ONLY>
-__device__ __forceinline__ void run_tile(const tfft_pass &p, int64_t tile, unsigned char *smem_raw)
+template <class A, int LOG_L, int B, bool L2ONLY, class LINE = CoreLine>
+__device__ __forceinline__ void run_tile(const tfft_pass &p, int64_t tile, unsigned char *smem_raw,
+                                         LINE line = LINE{})
 {
     using C = typename A::C;
     using SH = Shape<LOG_L>;
@@ -252,22 +265,23 @@ __device__ __forceinline__ void run_tile(const tfft_pass &p, int64_t tile, unsig
     const int64_t rest = tile / tiles0;
     const int64_t g1 = rest % p.n[1], g2 = rest / p.n[1];
     const bool live = g0 < p.n[0];
+    /* a line past the end of a ragged tile reads the last line again (no
+     * predicated loads: they cost 16 registers) and stores nothing */
+    const int64_t g0c = live ? g0 : p.n[0] - 1;
 
     using Store = typename A::Store;
     /* line bases from the stride or the per-line tables */
-    const int64_t t0 = p.tab0 && live ? __ldg(p.tab0 + g0) : -1;
+    const int64_t t0 = p.tab0 ? __ldg(p.tab0 + g0c) : -1;
     const int64_t t1 = p.tab1 ? __ldg(p.tab1 + g1) : -1;
-    const int64_t ibase = (t0 >= 0 ? t0 : g0 * p.is[0]) + (t1 >= 0 ? t1 : g1 * p.is[1]) +
+    const int64_t ibase = (t0 >= 0 ? t0 : g0c * p.is[0]) + (t1 >= 0 ? t1 : g1 * p.is[1]) +
                           g2 * p.is[2];
-    const int64_t obase = (t0 >= 0 ? t0 : g0 * p.os[0]) + (t1 >= 0 ? t1 : g1 * p.os[1]) +
+    const int64_t obase = (t0 >= 0 ? t0 : g0c * p.os[0]) + (t1 >= 0 ? t1 : g1 * p.os[1]) +
                           g2 * p.os[2];
     const Store *in = reinterpret_cast<const Store *>(p.in) + ibase;
     Store raw[E];
 #pragma unroll
     for (int q = 0; q < E; q++) {
-        if (!live) {
-            raw[q] = Store{};
-        } else if constexpr (L2ONLY) {
+        if constexpr (L2ONLY) {
             raw[q] = __ldcg(in + (int64_t)(j + q * TPL) * p.ies);
         } else {
             raw[q] = __ldcs(in + (int64_t)(j + q * TPL) * p.ies);
@@ -298,7 +312,7 @@ __device__ __forceinline__ void run_tile(const tfft_pass &p, int64_t tile, unsig
         a[q] = p.conj_in ? A::conj(v) : v;
     }
 
-    fft_line_regs<A, LOG_L, B>(a, sm, j, b, p.tw);
+    line.template run<A, LOG_L, B>(a, sm, j, b, p);
 
     if (p.post_tw) {
         const int64_t t = p.tw_level == 0 ? g0 : g1;
@@ -322,14 +336,16 @@ __device__ __forceinline__ void run_tile(const tfft_pass &p, int64_t tile, unsig
     }
 }
 
-/* double-float on FP64 storage: at least 16 resident warps per SM (a CTA of
- * W warps asks for 16/W CTAs per SM, which caps a thread at 128 registers);
- * the other arithmetics measured best with the compiler's own choice */
+/* Minimum CTAs per SM in the launch bounds.  0 leaves the register count to
+ * ptxas's default heuristic (128 for the double-float FP32 kernel, 80 for
+ * FP32); an explicit 1 lets it take up to 255 (225 and 161 registers: one CTA
+ * per SM, measured 20-35% slower).  The double-float FP64-storage kernel
+ * asks for 16 resident warps (16/W CTAs of W warps, at most 128 registers). */
 template <class A, int T>
 constexpr int pass_min_blocks()
 {
     constexpr int W = (T + 31) / 32;
-    return !A::kScaled || W >= 16 ? 1 : 16 / W;
+    return A::kScaled && W < 16 ? 16 / W : 0;
 }
 
 template <class A, int LOG_L, int B>
@@ -440,6 +456,8 @@ LaunchFn launcher_df32_2(int log_l, int log_b);
 LaunchFn launcher_df32_3(int log_l, int log_b);
 LaunchFn launcher_df32_4(int log_l, int log_b);
 LaunchFn launcher_df32_5(int log_l, int log_b);
+/* tensor form (fft_inst_tc.cu): one lines-per-CTA value per log2 L */
+LaunchFn launcher_tc(int log_l);
 
 } // namespace tfft
 

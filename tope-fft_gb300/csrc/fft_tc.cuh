@@ -1,0 +1,298 @@
+/*
+ * Split precision, tensor form: FP32 complex lines whose radix-16 Stockham
+ * stages run on the fifth-generation tensor cores (tcgen05) of sm_103a.
+ *
+ * A radix-16 stage computes, for every 16-point sub-transform (a "row"), the
+ * real product y = F x, where x holds the 32 reals of the twiddled inputs
+ * (re0, im0, re1, im1, ...) and F is the real 32x32 form of the DFT-16 (row
+ * 2k gives re X_k, row 2k+1 gives im X_k).  A CTA's rows go 128 at a time,
+ * one row per thread, into GEMMs D[128x32] = X[128x32] * F^T:
+ *   - x is split exactly into three BF16 pieces x0 + x1 + x2, each the top 8
+ *     significant bits of what the previous pieces left (an FP32 significand
+ *     has 24); F likewise from its FP32 rounding;
+ *   - D accumulates the six products with i + j <= 2, smallest first
+ *     (x2F0, x1F1, x0F2, x1F0, x0F1, x0F0), in FP32 in tensor memory; the
+ *     products left out are below 2^-24 of the result;
+ *   - the pieces of x go from registers to tensor memory (tcgen05.st, the A
+ *     operand in TMEM with lane = row); F's pieces sit in shared memory in
+ *     the canonical K-major layout without swizzle (the B operand, one
+ *     descriptor per 16-element K half);
+ *   - one thread issues the 12 MMAs (M = 128, N = 32, K = 16) of every group
+ *     and commits them to an mbarrier; every thread waits for it (bounded)
+ *     and reads its row of D back with tcgen05.ld.
+ * The twiddles (FP64-accurate hi/lo FP32 pairs), the first stage of radix
+ * 2^(log2 L mod 4), the stage exchange through shared memory and the
+ * load/store path are those of the FP32 pass kernel (ArithF32).
+ *
+ * A CTA holds 2^12 points (two row groups, 256 threads, 256 TMEM columns) or,
+ * for L = 2^13, 2^13 points (four groups, 512 threads, 512 columns).  Its
+ * dynamic shared memory is padded so that no more CTAs share an SM than its
+ * 512 TMEM columns serve.
+ */
+#pragma once
+#include <stdint.h>
+
+#include "fft_pass.cuh"
+
+namespace tfft {
+namespace tc {
+
+constexpr int kRows = 128;                            /* rows per MMA (M)          */
+constexpr int kDCols = 32;                            /* FP32 columns of D (N)     */
+constexpr int kAPieceCols = 16;                       /* 32 BF16 K values, packed  */
+constexpr int kGroupCols = kDCols + 3 * kAPieceCols;  /* TMEM columns per group    */
+constexpr int kBPieceBytes = 2048;                    /* 32 x 32 BF16              */
+constexpr int kBBytes = 3 * kBPieceBytes;
+constexpr int kWaitLimit = 1 << 22; /* mbarrier polls before a wait gives up */
+
+static_assert(kBBytes == TFFT_TC_MATRIX_BYTES, "matrix table size");
+
+/* shape of a CTA for log2 L: 2^12 points (2^13 for L = 2^13), one 16-point
+ * row per thread, TMEM columns for all row groups, and dynamic shared
+ * memory (data tile, F's pieces, mbarrier, TMEM address slot) padded so that
+ * at most 512 / TCOLS CTAs fit an SM */
+template <int LOG_L>
+struct Cfg {
+    static constexpr int TILE_LOG = LOG_L > 12 ? LOG_L : 12;
+    static constexpr int B = 1 << (TILE_LOG - LOG_L);
+    static constexpr int NT = (1 << TILE_LOG) / 16;
+    static constexpr int NG = NT / kRows;
+    static constexpr int TCOLS = NG * kGroupCols <= 256 ? 256 : 512;
+    static constexpr size_t TILE_BYTES =
+        (pass_smem_bytes<ArithF32, LOG_L, B>() + 1023) & ~(size_t)1023;
+    static constexpr size_t NEED = TILE_BYTES + kBBytes + 16;
+    static constexpr size_t FLOOR = TCOLS == 256 ? 80 * 1024 : 116 * 1024;
+    static constexpr size_t SMEM = NEED > FLOOR ? NEED : FLOOR;
+};
+
+/* byte offset of F[n][k] inside one piece: 8x8 core matrices of 16-bit
+ * values, each 8 rows (n) of 16 contiguous bytes (k); the next 8 rows lie
+ * 128 B further on (SBO), the next 8 k 512 B further on (LBO) */
+__host__ __device__ constexpr int b_offset(int n, int k)
+{
+    return (k >> 3) * 512 + (n >> 3) * 128 + (n & 7) * 16 + (k & 7) * 2;
+}
+
+/* instruction descriptor of kind::f16: D FP32, A and B BF16, both K-major,
+ * dense, N = 32, M = 128 */
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) |
+                            ((uint32_t)(kDCols >> 3) << 17) | ((uint32_t)(kRows >> 4) << 24);
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p)
+{
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+/* shared-memory descriptor of one K half of a piece: start address, LBO =
+ * 512 B, SBO = 128 B, descriptor version 1, no swizzle */
+__device__ __forceinline__ uint64_t b_desc(uint32_t addr)
+{
+    return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)(512 >> 4) << 16) |
+           ((uint64_t)(128 >> 4) << 32) | (1ull << 46);
+}
+
+__device__ __forceinline__ void fence_before()
+{
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void fence_after()
+{
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+/* x = three BF16 pieces, each packed as (re, im) into one 32-bit column:
+ * the low half is the even K element */
+__device__ __forceinline__ void split3(float2 v, uint32_t &p0, uint32_t &p1, uint32_t &p2)
+{
+    const uint32_t r0 = __float_as_uint(v.x), i0 = __float_as_uint(v.y);
+    p0 = __byte_perm(r0, i0, 0x7632);
+    const float r1 = __fsub_rn(v.x, __uint_as_float(r0 & 0xffff0000u));
+    const float i1 = __fsub_rn(v.y, __uint_as_float(i0 & 0xffff0000u));
+    const uint32_t ur1 = __float_as_uint(r1), ui1 = __float_as_uint(i1);
+    p1 = __byte_perm(ur1, ui1, 0x7632);
+    const float r2 = __fsub_rn(r1, __uint_as_float(ur1 & 0xffff0000u));
+    const float i2 = __fsub_rn(i1, __uint_as_float(ui1 & 0xffff0000u));
+    p2 = __byte_perm(__float_as_uint(r2), __float_as_uint(i2), 0x7632);
+}
+
+/* the three A pieces of this thread's row into its lane, columns
+ * col .. col + 47, then wait until they are written */
+__device__ __forceinline__ void store_pieces(uint32_t taddr, const uint32_t (&a)[16],
+                                             const uint32_t (&b)[16], const uint32_t (&c)[16])
+{
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%3, %4, %5, %6, %7, %8, %9, %10, %11, %12, "
+        "%13, %14, %15, %16, %17, %18};\n"
+        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%1], {%19, %20, %21, %22, %23, %24, %25, %26, %27, "
+        "%28, %29, %30, %31, %32, %33, %34};\n"
+        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%2], {%35, %36, %37, %38, %39, %40, %41, %42, %43, "
+        "%44, %45, %46, %47, %48, %49, %50};\n"
+        "tcgen05.wait::st.sync.aligned;\n" ::"r"(taddr),
+        "r"(taddr + kAPieceCols), "r"(taddr + 2 * kAPieceCols), "r"(a[0]), "r"(a[1]), "r"(a[2]),
+        "r"(a[3]), "r"(a[4]), "r"(a[5]), "r"(a[6]), "r"(a[7]), "r"(a[8]), "r"(a[9]), "r"(a[10]),
+        "r"(a[11]), "r"(a[12]), "r"(a[13]), "r"(a[14]), "r"(a[15]), "r"(b[0]), "r"(b[1]), "r"(b[2]),
+        "r"(b[3]), "r"(b[4]), "r"(b[5]), "r"(b[6]), "r"(b[7]), "r"(b[8]), "r"(b[9]), "r"(b[10]),
+        "r"(b[11]), "r"(b[12]), "r"(b[13]), "r"(b[14]), "r"(b[15]), "r"(c[0]), "r"(c[1]), "r"(c[2]),
+        "r"(c[3]), "r"(c[4]), "r"(c[5]), "r"(c[6]), "r"(c[7]), "r"(c[8]), "r"(c[9]), "r"(c[10]),
+        "r"(c[11]), "r"(c[12]), "r"(c[13]), "r"(c[14]), "r"(c[15])
+        : "memory");
+}
+
+/* this thread's row of D (32 FP32 columns), complete on return */
+__device__ __forceinline__ void load_row(uint32_t taddr, uint32_t (&d)[32])
+{
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, "
+        "%12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, "
+        "%30, %31}, [%32];\n"
+        "tcgen05.wait::ld.sync.aligned;\n"
+        : "=r"(d[0]), "=r"(d[1]), "=r"(d[2]), "=r"(d[3]), "=r"(d[4]), "=r"(d[5]), "=r"(d[6]),
+          "=r"(d[7]), "=r"(d[8]), "=r"(d[9]), "=r"(d[10]), "=r"(d[11]), "=r"(d[12]), "=r"(d[13]),
+          "=r"(d[14]), "=r"(d[15]), "=r"(d[16]), "=r"(d[17]), "=r"(d[18]), "=r"(d[19]),
+          "=r"(d[20]), "=r"(d[21]), "=r"(d[22]), "=r"(d[23]), "=r"(d[24]), "=r"(d[25]),
+          "=r"(d[26]), "=r"(d[27]), "=r"(d[28]), "=r"(d[29]), "=r"(d[30]), "=r"(d[31])
+        : "r"(taddr)
+        : "memory");
+}
+
+__device__ __forceinline__ void mma(uint32_t d, uint32_t a, uint64_t bdesc, uint32_t accumulate)
+{
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n}\n" ::"r"(d),
+        "r"(a), "l"(bdesc), "r"(kIdesc), "r"(accumulate)
+        : "memory");
+}
+
+__device__ __forceinline__ void commit(uint32_t mbar)
+{
+    asm volatile(
+        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar)
+        : "memory");
+}
+
+/* poll the mbarrier for the phase of the given parity; false if it did not
+ * complete within kWaitLimit polls */
+__device__ __forceinline__ bool wait_phase(uint32_t mbar, uint32_t parity)
+{
+    for (int it = 0; it < kWaitLimit; it++) {
+        uint32_t ok;
+        asm volatile(
+            "{\n.reg .pred P1;\nmbarrier.try_wait.parity.shared::cta.b64 P1, [%1], %2;\n"
+            "selp.b32 %0, 1, 0, P1;\n}\n"
+            : "=r"(ok)
+            : "r"(mbar), "r"(parity)
+            : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+
+/* the per-CTA state of the tensor stages */
+struct Ctx {
+    uint32_t tm;   /* TMEM base address (lane 0, first allocated column) */
+    uint32_t mbar; /* shared address of the MMA-completion mbarrier */
+    uint32_t bsm;  /* shared address of F's three pieces */
+    int *err;      /* set to 1 when a wait gives up */
+    uint32_t phase;
+};
+
+/*
+ * One radix-16 Stockham stage after NS points have been combined (the index
+ * arithmetic of tfft::stage with R = 16), the DFT-16 on the tensor cores.
+ */
+template <int LOG_L, int B, int NS, bool FROM_SMEM, bool TO_SMEM>
+__device__ __forceinline__ void stage16(float2 *a, float2 *sm, int j, int b, const void *tw, Ctx &cx)
+{
+    using A = ArithF32;
+    constexpr int L = 1 << LOG_L, TPL = L / 16, NT = TPL * B, NG = NT / kRows;
+    static_assert(NT % kRows == 0, "whole row groups");
+    if constexpr (FROM_SMEM) {
+#pragma unroll
+        for (int q = 0; q < 16; q++) a[q] = sm[sidx<B>(j + q * TPL, b)];
+    }
+    if constexpr (NS > 1) {
+        const int k = j & (NS - 1);
+#pragma unroll
+        for (int r = 1; r < 16; r++)
+            a[r] = A::mul_tw(a[r], A::load_tw(tw, (int64_t)(r * k) * (L / (NS * 16))));
+    }
+    const int t = threadIdx.x;
+    const uint32_t grp = cx.tm + (uint32_t)((t / kRows) * kGroupCols);
+    const uint32_t lane = (uint32_t)(t & 96) << 16; /* this warp's 32 TMEM lanes */
+    {
+        uint32_t x0[16], x1[16], x2[16];
+#pragma unroll
+        for (int r = 0; r < 16; r++) split3(a[r], x0[r], x1[r], x2[r]);
+        store_pieces(grp + lane + kDCols, x0, x1, x2);
+    }
+    fence_before();
+    __syncthreads();
+    if (t == 0) {
+        fence_after();
+        /* pieces (i of x, j of F), smallest products first */
+        constexpr int pi[6] = {2, 1, 0, 1, 0, 0}, pj[6] = {0, 1, 2, 0, 1, 0};
+#pragma unroll
+        for (int g = 0; g < NG; g++) {
+            const uint32_t d = cx.tm + (uint32_t)(g * kGroupCols);
+#pragma unroll
+            for (int s = 0; s < 6; s++)
+#pragma unroll
+                for (int h = 0; h < 2; h++)
+                    mma(d, d + kDCols + pi[s] * kAPieceCols + 8 * h,
+                        b_desc(cx.bsm + pj[s] * kBPieceBytes + h * 1024), (s | h) != 0);
+        }
+        commit(cx.mbar);
+    }
+    const bool ok = wait_phase(cx.mbar, cx.phase);
+    cx.phase ^= 1;
+    if (!ok) atomicExch(cx.err, 1);
+    fence_after();
+    {
+        uint32_t d[32];
+        load_row(grp + lane, d);
+#pragma unroll
+        for (int r = 0; r < 16; r++) a[r] = make_float2(__uint_as_float(d[2 * r]), __uint_as_float(d[2 * r + 1]));
+    }
+    if constexpr (TO_SMEM) {
+        const int k = j & (NS - 1);
+        const int o = (j / NS) * NS * 16 + k;
+#pragma unroll
+        for (int r = 0; r < 16; r++) sm[sidx<B>(o + r * NS, b)] = a[r];
+        __syncthreads();
+    }
+}
+
+/* radix-16 stages S .. NSTAGE-1 */
+template <int LOG_L, int B, int S>
+__device__ __forceinline__ void stages(float2 *a, float2 *sm, int j, int b, const void *tw, Ctx &cx)
+{
+    using SH = Shape<LOG_L>;
+    if constexpr (S < SH::NSTAGE) {
+        constexpr int first_log = SH::LR0 ? SH::LR0 : 4;
+        constexpr int NS = 1 << (first_log + 4 * (S - 1));
+        constexpr bool last = (S == SH::NSTAGE - 1);
+        stage16<LOG_L, B, NS, true, !last>(a, sm, j, b, tw, cx);
+        stages<LOG_L, B, S + 1>(a, sm, j, b, tw, cx);
+    }
+}
+
+/* run_tile's line transform for the tensor form (one tile per CTA) */
+struct Line {
+    Ctx cx;
+    template <class A, int LOG_L, int B>
+    __device__ __forceinline__ void run(float2 *a, float2 *sm, int j, int b, const tfft_pass &p)
+    {
+        static_assert(LOG_L >= 4, "a radix-16 stage needs 16 points");
+        using SH = Shape<LOG_L>;
+        if constexpr (SH::LR0) {
+            stage<ArithF32, LOG_L, B, SH::R0, 1, false, true>(a, sm, j, b, p.tw);
+        } else {
+            stage16<LOG_L, B, 1, false, (SH::NSTAGE > 1)>(a, sm, j, b, p.tw, cx);
+        }
+        stages<LOG_L, B, 1>(a, sm, j, b, p.tw, cx);
+    }
+};
+
+}  // namespace tc
+}  // namespace tfft

@@ -22,13 +22,16 @@ enum tfft_arith {
     TFFT_ARITH_DF32 = 3, /* split precision, accurate: FP32 storage, double-
                             float butterflies on chip, so only the FP32 loads
                             and stores round                                  */
+    TFFT_ARITH_TC = 4,   /* split precision, tensor: FP32 storage, radix-16
+                            stages as tcgen05 GEMMs on 3-way BF16 splits with
+                            FP32 accumulation; other stages as TFFT_ARITH_F32 */
 };
 
 /* bytes of one complex element in memory for an arithmetic */
 #define TFFT_ELEM_BYTES(arith) ((arith) >= TFFT_ARITH_F32 ? 8 : 16)
 
 /* Largest line length one CTA transforms: 2^13 complex points for 16-byte
- * on-chip elements, 2^14 for FP32 complex. */
+ * on-chip elements and for the tensor form, 2^14 for FP32 complex. */
 #define TFFT_MAX_LOG_L 14
 #define TFFT_MAX_LOG_L_ARITH(arith) ((arith) == TFFT_ARITH_F32 ? 14 : 13)
 
@@ -69,6 +72,9 @@ typedef struct tfft_pass {
      * replaces g1*is[1] (and g1*os[1]); used by batches of transforms that
      * sit at arbitrary offsets of the caller's packed buffer */
     const int64_t *tab0, *tab1;
+    /* TFFT_ARITH_TC: the 3 BF16 pieces of the real 32x32 DFT-16 matrix in
+     * the tensor cores' shared-memory layout (tfft_tc_matrix) */
+    const void *mma_b;
 } tfft_pass;
 
 /* ---- batches of independent transforms (persistent kernel) --------------- */
@@ -146,6 +152,17 @@ int tfft_quarter_table(void *tw, int n, void *stream);
 /* W_n^m for m < n, any n (DFT path) */
 int tfft_dft_table(void *tw, int n, void *stream);
 
+/* ---- tensor-core form ------------------------------------------------------ */
+/* bytes of the DFT-16 matrix table */
+#define TFFT_TC_MATRIX_BYTES 6144
+int tfft_tc_matrix(void *dst, void *stream);
+/* lines per CTA the tensor form needs for log2 L (its CTAs hold 2^12 points,
+ * 2^13 for L = 2^13) */
+int tfft_tc_b_tile(int log_l);
+/* read (and clear) the device's tensor-form error word: nonzero when a wait
+ * for the tensor cores gave up (synchronous on stream) */
+int tfft_tc_error(int *flag, void *stream);
+
 /* ---- kernels -------------------------------------------------------------- */
 int tfft_launch_pass(const tfft_pass *p, void *stream);
 /* can this (log_l, b_tile, arith) be launched? */
@@ -173,6 +190,18 @@ int tfft_bluestein_pre(const void *x, const void *chirp, void *w, int64_t n, int
 int tfft_pointwise(void *w, const void *h, int64_t m, void *stream);
 int tfft_bluestein_post(const void *w, const void *chirp, void *x, int64_t n, int conj_out,
                         double scale, void *stream);
+
+/* Real-data transforms of even length n = 2m through a complex transform of
+ * length m over the same bytes (FP64):
+ *   tables:   lo[i] = W_n^i (i < 2^shift), hi[h] = W_n^(h << shift), h <= m >> shift;
+ *   r2c_post: z = FFT_m of the packed reals, row by row (m complex) -> the
+ *             m + 1 non-redundant outputs x[0..m] of each row;
+ *   c2r_pre:  x[0..m] per row -> z, whose inverse FFT_m is the packed reals. */
+int tfft_real_tables(void *hi, void *lo, int64_t n, int shift, void *stream);
+int tfft_r2c_post(const void *z, void *x, const void *hi, const void *lo, int shift, int64_t m,
+                  int64_t rows, void *stream);
+int tfft_c2r_pre(const void *x, void *z, const void *hi, const void *lo, int shift, int64_t m,
+                 int64_t rows, void *stream);
 
 #ifdef __cplusplus
 }

@@ -177,7 +177,8 @@ void topeSetArith(struct topeFFT *f, int arith)
 
 void topeSetSplitMode(struct topeFFT *f, int mode)
 {
-    if (!f || (mode != TOPE_SPLIT_ACCURATE && mode != TOPE_SPLIT_FAST)) {
+    if (!f || (mode != TOPE_SPLIT_ACCURATE && mode != TOPE_SPLIT_FAST &&
+               mode != TOPE_SPLIT_TENSOR)) {
         set_status(f, TOPE_ERR_INVALID_ARG);
         return;
     }
@@ -185,10 +186,13 @@ void topeSetSplitMode(struct topeFFT *f, int mode)
     set_status(f, TOPE_SUCCESS);
 }
 
-/* arithmetic of FP32 plans: double-float on chip unless the fast mode */
+/* arithmetic of FP32 plans: double-float on chip unless the fast or the
+ * tensor-core mode */
 static int split_arith(const struct topeFFT *f)
 {
-    return (f && f->split_mode == TOPE_SPLIT_FAST) ? TFFT_ARITH_F32 : TFFT_ARITH_DF32;
+    if (f && f->split_mode == TOPE_SPLIT_FAST) return TFFT_ARITH_F32;
+    if (f && f->split_mode == TOPE_SPLIT_TENSOR) return TFFT_ARITH_TC;
+    return TFFT_ARITH_DF32;
 }
 
 /* ------------------------------------------------------------------------ */
@@ -226,6 +230,14 @@ typedef struct tope_impl {
     struct tope_impl *sub;
     void *chirp, *bhat;
     int64_t bl_m;
+    void *tc_matrix; /* tensor form: the DFT-16 matrix pieces */
+    /* real-data plan (R2C): the complex transform of length m = n/2 runs on
+     * the packed reals; spec holds the m + 1 outputs per row */
+    int real;
+    void *spec;
+    void *rtw_hi, *rtw_lo;
+    int rtw_shift;
+    int spec_cur; /* the spectrum, not the real array, is the current data */
     tope_evpair kev, mev;
     int pending;         /* kev recorded by an async exec, not yet accounted */
     int last_dir;
@@ -268,7 +280,7 @@ static size_t tw_elem_bytes(int arith) { (void)arith; return 16; }
 /* W_L table shared by every pass of length L */
 static int impl_wl_table(struct topeFFT *f, tope_impl *P, int log_l, const void **out)
 {
-    int key = log_l * 4 + P->arith;
+    int key = log_l * 8 + P->arith;
     for (int i = 0; i < P->ntabs; i++)
         if (P->tab_key[i] == key) {
             *out = P->tabs[i];
@@ -363,6 +375,11 @@ static int add_pass(struct topeFFT *f, tope_impl *P, int log_l, int64_t ies, int
     }
     int strided = (ies != 1) || (oes != 1);
     int b = (nl > 0) ? choose_b(log_l, p->n[0], strided) : 1;
+    if (P->arith == TFFT_ARITH_TC && log_l >= 4) {
+        /* the tensor form's CTA shape is fixed per length (ragged last tile) */
+        b = tfft_tc_b_tile(log_l);
+        p->mma_b = P->tc_matrix;
+    }
     p->b_tile = b;
     if (post_tw) {
         int lgn = ilog2_exact64(tw_n);
@@ -455,6 +472,10 @@ static void impl_free(tope_impl *P)
     tfft_free(P->dft_tab);
     tfft_free(P->chirp);
     tfft_free(P->bhat);
+    tfft_free(P->tc_matrix);
+    tfft_free(P->spec);
+    tfft_free(P->rtw_hi);
+    tfft_free(P->rtw_lo);
     impl_free(P->sub);
     tfft_free(P->buf[0]);
     tfft_free(P->buf[1]);
@@ -509,10 +530,11 @@ static int run_passes(struct topeFFT *f, tope_impl *P, int first, int count, int
 
 /* Build the device state of a plan and upload d (complex elements of the
  * arithmetic's storage type; arith < 0 takes the framework's setting).
- * Returns a status. */
+ * real: a 1D real-data plan of length 2x (x complex points carry the packed
+ * reals; FP64 storage only).  Returns a status. */
 static int impl_create(struct topeFFT *f, tope_impl **out, int ndim, int64_t x, int64_t y,
-                       int64_t z, int64_t batch, const void *d, int arith, uint64_t *t_pre,
-                       uint64_t *t_mem)
+                       int64_t z, int64_t batch, const void *d, int arith, int real,
+                       uint64_t *t_pre, uint64_t *t_mem)
 {
     *out = NULL;
     if (!f) return set_status(NULL, TOPE_ERR_INVALID_ARG);
@@ -550,7 +572,12 @@ static int impl_create(struct topeFFT *f, tope_impl **out, int ndim, int64_t x, 
 
     int lgx = ilog2_exact64(x), lgy = ilog2_exact64(y), lgz = ilog2_exact64(z);
     const int fp64_io = P->es == 16;
-    if (ndim == 1 && x == 2 && batch == 1 && fp64_io) P->mode = MODE_N2;
+    P->real = real;
+    if (real && (ndim != 1 || !fp64_io)) {
+        impl_free(P);
+        return set_status(f, TOPE_ERR_UNSUPPORTED);
+    }
+    if (ndim == 1 && x == 2 && batch == 1 && fp64_io && !real) P->mode = MODE_N2;
     else if (ndim == 1 && lgx < 0)
         P->mode = !(batch == 1 && fp64_io) ? -1 : x < BLUESTEIN_MIN_N ? MODE_DFT : MODE_BLUESTEIN;
     else if (lgx < 0 || lgy < 0 || lgz < 0) P->mode = -1;
@@ -572,6 +599,10 @@ static int impl_create(struct topeFFT *f, tope_impl **out, int ndim, int64_t x, 
     tfft_event_record(w->pair.a, stream);
     tfft_event_record(P->kev.a, stream);
     if (P->mode == MODE_FFT) {
+        if (P->arith == TFFT_ARITH_TC) {
+            if (tfft_malloc(&P->tc_matrix, TFFT_TC_MATRIX_BYTES)) st = set_status(f, TOPE_ERR_ALLOC);
+            else if ((rc = tfft_tc_matrix(P->tc_matrix, stream))) st = cuda_status(f, rc);
+        }
         for (int a = 0; a < 3 && !st; a++) st = plan_axis(f, P, a);
         int need2 = 0;
         for (int i = 0; i < P->npass; i++) need2 |= P->oop[i];
@@ -604,7 +635,7 @@ static int impl_create(struct topeFFT *f, tope_impl **out, int ndim, int64_t x, 
         while (m < 2 * x - 1) m <<= 1;
         P->bl_m = m;
         uint64_t t0 = 0, t1 = 0;
-        st = impl_create(f, &P->sub, 1, m, 1, 1, 1, NULL, P->arith, &t0, &t1);
+        st = impl_create(f, &P->sub, 1, m, 1, 1, 1, NULL, P->arith, 0, &t0, &t1);
         if (!st) {
             f->live_plans--; /* the sub-plan lives and dies with this plan */
             if (tfft_malloc(&P->chirp, 16 * (size_t)x) || tfft_malloc(&P->bhat, 16 * (size_t)m))
@@ -621,6 +652,19 @@ static int impl_create(struct topeFFT *f, tope_impl **out, int ndim, int64_t x, 
         if (tfft_malloc((void **)&P->bitrev[0], 2 * sizeof(int)))
             st = set_status(f, TOPE_ERR_ALLOC);
         else if ((rc = tfft_bitrev_table(P->bitrev[0], 1, stream)))
+            st = cuda_status(f, rc);
+    }
+    if (!st && real) {
+        /* spectrum rows of x + 1 points; W_{2x}^k from two tables of about
+         * sqrt(2x) entries each */
+        int shift = 0;
+        while (((int64_t)1 << (2 * shift)) < 2 * x) shift++;
+        P->rtw_shift = shift;
+        const size_t nhi = (size_t)(x >> shift) + 1;
+        if (tfft_malloc(&P->spec, 16 * (size_t)(x + 1) * (size_t)batch) ||
+            tfft_malloc(&P->rtw_hi, 16 * nhi) || tfft_malloc(&P->rtw_lo, (size_t)16 << shift))
+            st = set_status(f, TOPE_ERR_ALLOC);
+        else if ((rc = tfft_real_tables(P->rtw_hi, P->rtw_lo, 2 * x, shift, stream)))
             st = cuda_status(f, rc);
     }
     tfft_event_record(P->kev.b, stream);
@@ -711,7 +755,17 @@ static int impl_exec_async(struct topeFFT *f, tope_impl *P, int dir)
     tope_fw *w = fw_of(f);
     tfft_event_record(P->kev.a, stream);
     tfft_event_record(w->pair.a, stream);
-    if (P->mode == MODE_FFT) {
+    const int64_t rows = P->c[3], m = P->c[0];
+    if (P->real && dir == INVERSE) {
+        /* spectrum -> packed spectrum of the half-length transform */
+        if ((rc = tfft_c2r_pre(P->spec, P->buf[P->cur], P->rtw_hi, P->rtw_lo, P->rtw_shift, m,
+                               rows, stream)))
+            st = cuda_status(f, rc);
+        P->spec_cur = 0;
+    }
+    if (st) {
+        /* nothing more to queue */
+    } else if (P->mode == MODE_FFT) {
         double scale = dir == INVERSE ? 1.0 / (double)P->volume : 1.0;
         if (P->npass == 0) {
             /* all axes of length 1: identity (inverse divides by 1) */
@@ -740,10 +794,27 @@ static int impl_exec_async(struct topeFFT *f, tope_impl *P, int dir)
                                              inv ? 1.0 / (double)n : 1.0, stream)))
             st = cuda_status(f, rc);
     }
+    if (!st && P->real && dir == FORWARD) {
+        if ((rc = tfft_r2c_post(P->buf[P->cur], P->spec, P->rtw_hi, P->rtw_lo, P->rtw_shift, m,
+                                rows, stream)))
+            st = cuda_status(f, rc);
+        P->spec_cur = 1;
+    }
     tfft_event_record(P->kev.b, stream);
     tfft_event_record(w->pair.b, stream);
     P->pending = 1;
     return st;
+}
+
+/* the plan's current data: its device buffer and size in bytes */
+static void *cur_data(const tope_impl *P, size_t *bytes)
+{
+    if (P->real && P->spec_cur) {
+        *bytes = (size_t)16 * (size_t)(P->c[0] + 1) * (size_t)P->c[3];
+        return P->spec;
+    }
+    *bytes = (size_t)P->total * P->es;
+    return P->buf[P->cur];
 }
 
 /* synchronous: exec, then read back into d (if non-NULL).  es_caller is the
@@ -765,8 +836,10 @@ static int impl_exec(struct topeFFT *f, tope_impl *P, void *d, int es_caller, in
         return st;
     }
     if (d) {
+        size_t nb;
+        void *src = cur_data(P, &nb);
         tfft_event_record(P->mev.a, stream);
-        rc = tfft_d2h(d, P->buf[P->cur], (size_t)P->total * P->es, stream);
+        rc = tfft_d2h(d, src, nb, stream);
         tfft_event_record(P->mev.b, stream);
         if (rc) {
             tfft_stream_sync(stream);
@@ -779,6 +852,12 @@ static int impl_exec(struct topeFFT *f, tope_impl *P, void *d, int es_caller, in
         uint64_t ns = 0;
         tfft_event_elapsed_ns(P->mev.a, P->mev.b, &ns);
         *t_mem += ns;
+    }
+    if (P->arith == TFFT_ARITH_TC) {
+        /* a wait for the tensor cores that gave up leaves a flag */
+        int flag = 0;
+        if ((rc = tfft_tc_error(&flag, stream))) return cuda_status(f, rc);
+        if (flag) return set_status(f, TOPE_ERR_TIMEOUT);
     }
     return set_status(f, TOPE_SUCCESS);
 }
@@ -814,6 +893,7 @@ static int impl_upload(struct topeFFT *f, tope_impl *P, const void *d, int es_ca
 {
     if (!d || P->es != es_caller) return set_status(f, TOPE_ERR_INVALID_ARG);
     void *stream = f->command_queue;
+    P->spec_cur = 0; /* a real-data plan takes its real array here */
     tfft_event_record(P->mev.a, stream);
     int rc = tfft_h2d(P->buf[P->cur], d, (size_t)P->total * P->es, stream);
     tfft_event_record(P->mev.b, stream);
@@ -830,8 +910,10 @@ static int impl_download(struct topeFFT *f, tope_impl *P, void *d, int es_caller
 {
     if (!d || P->es != es_caller) return set_status(f, TOPE_ERR_INVALID_ARG);
     void *stream = f->command_queue;
+    size_t nb;
+    void *src = cur_data(P, &nb);
     tfft_event_record(P->mev.a, stream);
-    int rc = tfft_d2h(d, P->buf[P->cur], (size_t)P->total * P->es, stream);
+    int rc = tfft_d2h(d, src, nb, stream);
     tfft_event_record(P->mev.b, stream);
     if (!rc) rc = tfft_stream_sync(stream);
     if (rc) return cuda_status(f, rc);
@@ -862,15 +944,23 @@ static void plan1d(struct topeFFT *f, struct topePlan1D *t, int x, int batch, in
     t->x = x;
     t->type = type;
     t->dim = 1;
-    if (type != C2C) {
+    /* R2C (topefft.h defines it; the reference implements only C2C): x real
+     * points per row in, x/2 + 1 complex points per row out */
+    const int real = type == R2C;
+    if (type != C2C && !real) {
         set_status(f, TOPE_ERR_UNSUPPORTED);
+        return;
+    }
+    if (real && (x < 2 || x % 2)) {
+        set_status(f, TOPE_ERR_INVALID_SIZE);
         return;
     }
     int lg = ilog2_exact64(x);
     t->radix = lg >= 0 ? ref_radix(lg) : -1;
     t->log = lg >= 0 ? ref_stages(lg) : 0;
     tope_impl *P;
-    if (impl_create(f, &P, 1, x, 1, 1, batch, d, arith, &t->totalPreKernel, &t->totalMemory))
+    if (impl_create(f, &P, 1, real ? x / 2 : x, 1, 1, batch, d, arith, real, &t->totalPreKernel,
+                    &t->totalMemory))
         return;
     t->impl = P;
     t->dataSize = (size_t)P->total * P->es;
@@ -934,6 +1024,30 @@ void tope1DDownload(struct topeFFT *f, struct topePlan1D *t, double *d)
     if (P) impl_download(f, P, d, 16, &t->totalKernel, &t->totalMemory);
 }
 
+void tope1DUploadSpectrum(struct topeFFT *f, struct topePlan1D *t, const double *spec)
+{
+    tope_impl *P = t ? impl_of(f, t->impl) : NULL;
+    if (!P) return;
+    if (!P->real || !spec) {
+        set_status(f, TOPE_ERR_INVALID_ARG);
+        return;
+    }
+    void *stream = f->command_queue;
+    tfft_event_record(P->mev.a, stream);
+    int rc = tfft_h2d(P->spec, spec, (size_t)16 * (size_t)(P->c[0] + 1) * (size_t)P->c[3], stream);
+    tfft_event_record(P->mev.b, stream);
+    if (!rc) rc = tfft_stream_sync(stream);
+    if (rc) {
+        cuda_status(f, rc);
+        return;
+    }
+    P->spec_cur = 1;
+    uint64_t ns = 0;
+    tfft_event_elapsed_ns(P->mev.a, P->mev.b, &ns);
+    t->totalMemory += ns;
+    set_status(f, TOPE_SUCCESS);
+}
+
 void tope1DDestroy(struct topeFFT *f, struct topePlan1D *t)
 {
     tope_impl *P = t ? impl_of(f, t->impl) : NULL;
@@ -972,7 +1086,8 @@ static void plan2d(struct topeFFT *f, struct topePlan2D *t, int x, int y, int ty
     t->logX = ref_stages(lx);
     t->logY = ref_stages(ly);
     tope_impl *P;
-    if (impl_create(f, &P, 2, x, y, 1, 1, d, arith, &t->totalPreKernel, &t->totalMemory)) return;
+    if (impl_create(f, &P, 2, x, y, 1, 1, d, arith, 0, &t->totalPreKernel, &t->totalMemory))
+        return;
     t->impl = P;
     t->dataSize = (size_t)P->total * P->es;
     t->bitX = P->bitrev[0];
@@ -1085,7 +1200,8 @@ static void plan3d(struct topeFFT *f, struct topePlan3D *t, int x, int y, int z,
     t->logY = ref_stages(ly);
     t->logZ = ref_stages(lz);
     tope_impl *P;
-    if (impl_create(f, &P, 3, x, y, z, 1, d, arith, &t->totalPreKernel, &t->totalMemory)) return;
+    if (impl_create(f, &P, 3, x, y, z, 1, d, arith, 0, &t->totalPreKernel, &t->totalMemory))
+        return;
     t->impl = P;
     t->dataSize = (size_t)P->total * P->es;
     t->bitX = P->bitrev[0];

@@ -34,7 +34,7 @@ TOPE_ERR_DESTROYED = 6
 TOPE_ERR_UNSUPPORTED = 7
 TOPE_ERR_TIMEOUT = 8
 TOPE_ARITH_FP64, TOPE_ARITH_DF64 = 0, 1
-TOPE_SPLIT_ACCURATE, TOPE_SPLIT_FAST = 0, 1
+TOPE_SPLIT_ACCURATE, TOPE_SPLIT_FAST, TOPE_SPLIT_TENSOR = 0, 1, 2
 
 LIB_PATH = Path(__file__).resolve().parent / "libtopefft.so"
 
@@ -127,6 +127,7 @@ SIGNATURES = [
     ("tope3DExecDevice", None, [_F, _P3, C.c_int]),
     ("tope1DUpload", None, [_F, _P1, _D]),
     ("tope1DDownload", None, [_F, _P1, _D]),
+    ("tope1DUploadSpectrum", None, [_F, _P1, _D]),
     ("tope2DUpload", None, [_F, _P2, _D]),
     ("tope2DDownload", None, [_F, _P2, _D]),
     ("tope3DUpload", None, [_F, _P3, _D]),
@@ -294,6 +295,11 @@ def download(f, t, d) -> None:
     fn = {TopePlan1D: lib.tope1DDownload, TopePlan2D: lib.tope2DDownload,
           TopePlan3D: lib.tope3DDownload}[type(t)]
     fn(C.byref(f), C.byref(t), _ptr(d))
+
+
+def upload_spectrum(f, t, spec) -> None:
+    """R2C plans: the x/2 + 1 complex outputs per row, for an inverse."""
+    lib.tope1DUploadSpectrum(C.byref(f), C.byref(t), _ptr(spec))
 
 
 def topeSync(f) -> None:
