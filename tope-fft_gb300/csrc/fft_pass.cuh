@@ -145,7 +145,7 @@ struct Shape {
 };
 
 template <class A, int LOG_L, int B>
-constexpr size_t pass_smem_bytes()
+__host__ __device__ constexpr size_t pass_smem_bytes()
 {
     return Shape<LOG_L>::TPL > 1
                ? (size_t)((1 << LOG_L) + ((1 << LOG_L) >> 4)) * B * sizeof(typename A::S)
@@ -239,54 +239,52 @@ struct CoreLine {
     }
 };
 
+/* where one thread's line of a tile lives */
+struct TileGeom {
+    int64_t g0, g1;       /* line coordinates (g0 may lie past n[0]) */
+    int64_t ibase, obase; /* first element of the input and output line */
+    bool live;            /* g0 < n[0]: the line exists and is stored */
+};
+
 /*
- * One tile: lines tile*B .. tile*B+B-1 of the pass's g0 dimension (the last
- * tile may be ragged: its missing lines compute on a copy of the last line
- * and store nothing),
- * for the g1/g2 coordinates encoded in tile.  L2ONLY selects loads that
- * bypass L1 (ld.global.cg): needed when another CTA of the same launch
- * wrote the data (the persistent batch kernel); a plain pass launch reads
- * with the streaming hint.  LINE transforms the loaded points (CoreLine, or
- * the tensor-core stages of fft_tc.cuh).
+ * Lines tile*B .. tile*B+B-1 of the pass's g0 dimension (the last tile may be
+ * ragged: its missing lines compute on a copy of the last line and store
+ * nothing), for the g1/g2 coordinates encoded in tile; b is this thread's
+ * line within the tile.
  */
-template <class A, int LOG_L, int B, bool L2ONLY, class LINE = CoreLine>
-__device__ __forceinline__ void run_tile(const tfft_pass &p, int64_t tile, unsigned char *smem_raw,
-                                         LINE line = LINE{})
+template <int B>
+__device__ __forceinline__ TileGeom tile_geom(const tfft_pass &p, int64_t tile, int b)
+{
+    TileGeom g;
+    const int64_t tiles0 = (p.n[0] + B - 1) / B;
+    g.g0 = (tile % tiles0) * B + b;
+    const int64_t rest = tile / tiles0;
+    g.g1 = rest % p.n[1];
+    const int64_t g2 = rest / p.n[1];
+    g.live = g.g0 < p.n[0];
+    /* a line past the end of a ragged tile reads the last line again (no
+     * predicated loads: they cost 16 registers) and stores nothing */
+    const int64_t g0c = g.live ? g.g0 : p.n[0] - 1;
+    /* line bases from the strides or the per-line tables */
+    const int64_t t0 = p.tab0 ? __ldg(p.tab0 + g0c) : -1;
+    const int64_t t1 = p.tab1 ? __ldg(p.tab1 + g.g1) : -1;
+    g.ibase = (t0 >= 0 ? t0 : g0c * p.is[0]) + (t1 >= 0 ? t1 : g.g1 * p.is[1]) + g2 * p.is[2];
+    g.obase = (t0 >= 0 ? t0 : g0c * p.os[0]) + (t1 >= 0 ? t1 : g.g1 * p.os[1]) + g2 * p.os[2];
+    return g;
+}
+
+/* Everything after the loads: the tile scaling of the double-float FP64
+ * arithmetic, conjugation, the line transform, the four-step twiddle, and
+ * the store (conjugation and scale fused) */
+template <class A, int LOG_L, int B, class LINE>
+__device__ __forceinline__ void finish_tile(const tfft_pass &p, const TileGeom &g,
+                                            typename A::Store (&raw)[Shape<LOG_L>::E],
+                                            typename A::S *sm, int j, int b, LINE &line)
 {
     using C = typename A::C;
     using SH = Shape<LOG_L>;
-    constexpr int E = SH::E, TPL = SH::TPL;
-    typename A::S *sm = reinterpret_cast<typename A::S *>(smem_raw);
-
-    const int tid = threadIdx.x;
-    const int b = tid % B, j = tid / B;
-    const int64_t tiles0 = (p.n[0] + B - 1) / B;
-    const int64_t g0 = (tile % tiles0) * B + b;
-    const int64_t rest = tile / tiles0;
-    const int64_t g1 = rest % p.n[1], g2 = rest / p.n[1];
-    const bool live = g0 < p.n[0];
-    /* a line past the end of a ragged tile reads the last line again (no
-     * predicated loads: they cost 16 registers) and stores nothing */
-    const int64_t g0c = live ? g0 : p.n[0] - 1;
-
     using Store = typename A::Store;
-    /* line bases from the stride or the per-line tables */
-    const int64_t t0 = p.tab0 ? __ldg(p.tab0 + g0c) : -1;
-    const int64_t t1 = p.tab1 ? __ldg(p.tab1 + g1) : -1;
-    const int64_t ibase = (t0 >= 0 ? t0 : g0c * p.is[0]) + (t1 >= 0 ? t1 : g1 * p.is[1]) +
-                          g2 * p.is[2];
-    const int64_t obase = (t0 >= 0 ? t0 : g0c * p.os[0]) + (t1 >= 0 ? t1 : g1 * p.os[1]) +
-                          g2 * p.os[2];
-    const Store *in = reinterpret_cast<const Store *>(p.in) + ibase;
-    Store raw[E];
-#pragma unroll
-    for (int q = 0; q < E; q++) {
-        if constexpr (L2ONLY) {
-            raw[q] = __ldcg(in + (int64_t)(j + q * TPL) * p.ies);
-        } else {
-            raw[q] = __ldcs(in + (int64_t)(j + q * TPL) * p.ies);
-        }
-    }
+    constexpr int E = SH::E, TPL = SH::TPL;
     /* arithmetics with a narrower exponent range than their storage work on
      * the tile scaled by 2^-delta, delta = the tile's largest FP64 exponent */
     int delta = 0, delta_out = 0;
@@ -315,7 +313,7 @@ __device__ __forceinline__ void run_tile(const tfft_pass &p, int64_t tile, unsig
     line.template run<A, LOG_L, B>(a, sm, j, b, p);
 
     if (p.post_tw) {
-        const int64_t t = p.tw_level == 0 ? g0 : g1;
+        const int64_t t = p.tw_level == 0 ? g.g0 : g.g1;
         const int64_t mask = (int64_t(1) << p.tw_shift) - 1;
 #pragma unroll
         for (int q = 0; q < E; q++) {
@@ -326,14 +324,44 @@ __device__ __forceinline__ void run_tile(const tfft_pass &p, int64_t tile, unsig
         }
     }
 
-    Store *out = reinterpret_cast<Store *>(p.out) + obase;
-    if (live) {
+    Store *out = reinterpret_cast<Store *>(p.out) + g.obase;
+    if (g.live) {
 #pragma unroll
         for (int q = 0; q < E; q++) {
             C v = p.conj_out ? A::conj(a[q]) : a[q];
             __stcs(out + (int64_t)(j + q * TPL) * p.oes, A::store_s(v, delta_out, p.scale));
         }
     }
+}
+
+/*
+ * One tile, loaded straight into registers.  L2ONLY selects loads that
+ * bypass L1 (ld.global.cg): needed when another CTA of the same launch wrote
+ * the data (the persistent batch kernel); a plain pass launch reads with the
+ * streaming hint.  LINE transforms the loaded points (CoreLine, or the
+ * tensor-core stages of fft_tc.cuh).
+ */
+template <class A, int LOG_L, int B, bool L2ONLY, class LINE = CoreLine>
+__device__ __forceinline__ void run_tile(const tfft_pass &p, int64_t tile, unsigned char *smem_raw,
+                                         LINE line = LINE{})
+{
+    using SH = Shape<LOG_L>;
+    using Store = typename A::Store;
+    constexpr int E = SH::E, TPL = SH::TPL;
+    typename A::S *sm = reinterpret_cast<typename A::S *>(smem_raw);
+    const int b = threadIdx.x % B, j = threadIdx.x / B;
+    const TileGeom g = tile_geom<B>(p, tile, b);
+    const Store *in = reinterpret_cast<const Store *>(p.in) + g.ibase;
+    Store raw[E];
+#pragma unroll
+    for (int q = 0; q < E; q++) {
+        if constexpr (L2ONLY) {
+            raw[q] = __ldcg(in + (int64_t)(j + q * TPL) * p.ies);
+        } else {
+            raw[q] = __ldcs(in + (int64_t)(j + q * TPL) * p.ies);
+        }
+    }
+    finish_tile<A, LOG_L, B>(p, g, raw, sm, j, b, line);
 }
 
 /* Minimum CTAs per SM in the launch bounds.  0 leaves the register count to
