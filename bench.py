@@ -370,8 +370,6 @@ def run_gpu(args, wl: dict) -> dict:
     for _ in range(args.warmup):
         step()
     T.topeSync(f)
-    T.topeSetPassTiming(f, 1)
-    T.topeResetPassTimes(f, t)
     sampler = ClockSampler(local)
     sampler.start()
     if dist is not None:
@@ -389,13 +387,23 @@ def run_gpu(args, wl: dict) -> dict:
     clocks = sampler.stop()
     T.check(f)
     ms_local = e0.elapsed_time(e1) / args.steps
-    passes = T.pass_times(f, t)
-    T.topeSetPassTiming(f, 0)
     ms, value = aggregate(dist, ms_local, flops_per_step(wl), device=torch.device("cuda", local))
     value_gflops = value / 1e9
-    launches = sum(p["launches"] for p in passes)
 
-    # accuracy after W+K round trips (forward then inverse each step)
+    # per-launch kernel times for the roofline, in a separate loop: the event
+    # pair around every launch would otherwise add to small steps' time
+    pt_steps = max(1, min(args.steps, 10))
+    T.topeSetPassTiming(f, 1)
+    T.topeResetPassTimes(f, t)
+    for _ in range(pt_steps):
+        step()
+    T.topeSync(f)
+    T.check(f)
+    passes = T.pass_times(f, t)
+    T.topeSetPassTiming(f, 0)
+    launches = sum(p["launches"] for p in passes) * args.steps // pt_steps
+
+    # accuracy after all the round trips above (forward then inverse each step)
     back = np.empty_like(xs)
     (T.downloadF32 if f32 else T.download)(f, t, back)
     xs64 = xs.astype(np.float64)

@@ -68,9 +68,11 @@ void tope3DDownload(struct topeFFT *f, struct topePlan3D *t, double *d);
 void topeSync(struct topeFFT *f);
 
 /* ---- batched 1D ----------------------------------------------------------- */
-/* batch contiguous transforms of length x (row b at d + 2*b*x).  The plan is
- * a topePlan1D; tope1DExec / tope1DExecDevice / Upload / Download / Destroy
- * apply to all rows.  dataSize = 16*x*batch. */
+/* batch contiguous transforms of length x (row b at d + 2*b*x), any x >= 1
+ * (lengths that are not powers of two run as an O(x^2) DFT below 128 points
+ * and as Bluestein convolutions above).  The plan is a topePlan1D;
+ * tope1DExec / tope1DExecDevice / Upload / Download / Destroy apply to all
+ * rows.  dataSize = 16*x*batch. */
 void tope1DBatchPlanInit(struct topeFFT *f, struct topePlan1D *t, int x, int batch, int type,
                          double *d);
 

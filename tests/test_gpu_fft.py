@@ -158,6 +158,19 @@ def test_1d_non_power_of_two_long(T, fw, orc, n):
             assert orc.rel_l2(got, orc.dft_ld(x, n, dir_)) <= tol
 
 
+@pytest.mark.parametrize("n,b", [(3, 5), (100, 3), (127, 2), (1000, 4), (4095, 3), (10007, 2)])
+def test_1d_non_power_of_two_batched(T, fw, orc, n, b):
+    """Batched rows of a non-power-of-two length (the DFT below 128 points,
+    Bluestein from 128 on), each row against the long-double oracle."""
+    x = orc.uniform(n * b, SEED0 + 11 * n)
+    tol = 1e-13 * np.log2(n)
+    for dir_ in (1, 0):
+        got = run1d(T, fw, x, n, dir_, batch=b)
+        want = np.concatenate([orc.bluestein_ld(x[2 * n * i: 2 * n * (i + 1)], n, dir_)
+                               for i in range(b)])
+        assert orc.rel_l2(got, want) <= tol
+
+
 def test_1d_non_power_of_two_round_trip(T, fw, orc):
     n = 1000003
     x = orc.uniform(n, SEED0 + 8)

@@ -139,23 +139,26 @@ __global__ void k_dft_table(double2 *tw, int n)
 
 /* out[k] = sum_j in[j] W_n^{jk}; twiddle index advanced modulo n exactly */
 __global__ void k_dft(const double2 *__restrict__ in, double2 *__restrict__ out,
-                      const double2 *__restrict__ tw, int n, int dir)
+                      const double2 *__restrict__ tw, int n, int dir, int64_t rows)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
-    double sr = 0.0, si = 0.0;
-    int m = 0;
-    for (int j = 0; j < n; j++) {
-        const double2 x = in[j];
-        double2 w = __ldg(tw + m);
-        if (!dir) w.y = -w.y;
-        sr = fma(x.x, w.x, fma(-x.y, w.y, sr));
-        si = fma(x.x, w.y, fma(x.y, w.x, si));
-        m += k;
-        if (m >= n) m -= n;
+    for (int64_t r = blockIdx.y; r < rows; r += gridDim.y) {
+        const double2 *x_row = in + r * n;
+        double sr = 0.0, si = 0.0;
+        int m = 0;
+        for (int j = 0; j < n; j++) {
+            const double2 x = x_row[j];
+            double2 w = __ldg(tw + m);
+            if (!dir) w.y = -w.y;
+            sr = fma(x.x, w.x, fma(-x.y, w.y, sr));
+            si = fma(x.x, w.y, fma(x.y, w.x, si));
+            m += k;
+            if (m >= n) m -= n;
+        }
+        const double s = dir ? 1.0 : 1.0 / (double)n;
+        out[r * n + k] = make_double2(sr * s, si * s);
     }
-    const double s = dir ? 1.0 : 1.0 / (double)n;
-    out[k] = make_double2(sr * s, si * s);
 }
 
 /* In-place bit-reversal permutation along an axis, the reference's swap
@@ -211,38 +214,44 @@ __global__ void k_bluestein_b(double2 *b, const double2 *__restrict__ c, int64_t
     }
 }
 
-/* w[k] = x[k] c[k] (x conjugated first for an inverse), zero-padded to m */
+/* per row: w[k] = x[k] c[k] (x conjugated first for an inverse), zero-padded to m */
 __global__ void k_bluestein_pre(const double2 *__restrict__ x, const double2 *__restrict__ c,
-                                double2 *__restrict__ w, int64_t n, int64_t m, int conj_in)
+                                double2 *__restrict__ w, int64_t n, int64_t m, int conj_in,
+                                int64_t rows)
 {
-    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < m;
-         k += (int64_t)gridDim.x * blockDim.x) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m * rows;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = i / m, k = i - r * m;
         double2 v = make_double2(0.0, 0.0);
         if (k < n) {
-            double2 a = x[k];
+            double2 a = x[r * n + k];
             if (conj_in) a.y = -a.y;
             v = cmul(a, c[k]);
         }
-        w[k] = v;
+        w[i] = v;
     }
 }
 
-__global__ void k_pointwise(double2 *__restrict__ w, const double2 *__restrict__ h, int64_t m)
+/* w *= h, h of length m shared by every row */
+__global__ void k_pointwise(double2 *__restrict__ w, const double2 *__restrict__ h, int64_t m,
+                            int64_t rows)
 {
-    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < m;
-         k += (int64_t)gridDim.x * blockDim.x)
-        w[k] = cmul(w[k], h[k]);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m * rows;
+         i += (int64_t)gridDim.x * blockDim.x)
+        w[i] = cmul(w[i], h[i % m]);
 }
 
-/* x[k] = w[k] c[k], conjugated and scaled for an inverse */
+/* per row: x[k] = w[k] c[k], conjugated and scaled for an inverse */
 __global__ void k_bluestein_post(const double2 *__restrict__ w, const double2 *__restrict__ c,
-                                 double2 *__restrict__ x, int64_t n, int conj_out, double scale)
+                                 double2 *__restrict__ x, int64_t n, int64_t m, int conj_out,
+                                 double scale, int64_t rows)
 {
-    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
-         k += (int64_t)gridDim.x * blockDim.x) {
-        double2 v = cmul(w[k], c[k]);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n * rows;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = i / n, k = i - r * n;
+        double2 v = cmul(w[r * m + k], c[k]);
         if (conj_out) v.y = -v.y;
-        x[k] = make_double2(v.x * scale, v.y * scale);
+        x[i] = make_double2(v.x * scale, v.y * scale);
     }
 }
 
@@ -367,10 +376,12 @@ int tfft_dft_table(void *tw, int n, void *s)
     return (int)cudaGetLastError();
 }
 
-int tfft_launch_dft(const void *in, void *out, const void *tw, int n, int dir, void *s)
+int tfft_launch_dft(const void *in, void *out, const void *tw, int n, int dir, int64_t rows,
+                    void *s)
 {
-    k_dft<<<(n + 127) / 128, 128, 0, (cudaStream_t)s>>>((const double2 *)in, (double2 *)out,
-                                                       (const double2 *)tw, n, dir);
+    const dim3 grid((unsigned)((n + 127) / 128), (unsigned)(rows < 65535 ? rows : 65535));
+    k_dft<<<grid, 128, 0, (cudaStream_t)s>>>((const double2 *)in, (double2 *)out,
+                                             (const double2 *)tw, n, dir, rows);
     return (int)cudaGetLastError();
 }
 
@@ -392,24 +403,25 @@ int tfft_bluestein_tables(void *chirp, void *b, int64_t n, int64_t m, void *s)
 }
 
 int tfft_bluestein_pre(const void *x, const void *chirp, void *w, int64_t n, int64_t m,
-                       int conj_in, void *s)
+                       int conj_in, int64_t rows, void *s)
 {
-    k_bluestein_pre<<<grid_for(m, 256), 256, 0, (cudaStream_t)s>>>(
-        (const double2 *)x, (const double2 *)chirp, (double2 *)w, n, m, conj_in);
+    k_bluestein_pre<<<grid_for(m * rows, 256), 256, 0, (cudaStream_t)s>>>(
+        (const double2 *)x, (const double2 *)chirp, (double2 *)w, n, m, conj_in, rows);
     return (int)cudaGetLastError();
 }
 
-int tfft_pointwise(void *w, const void *h, int64_t m, void *s)
+int tfft_pointwise(void *w, const void *h, int64_t m, int64_t rows, void *s)
 {
-    k_pointwise<<<grid_for(m, 256), 256, 0, (cudaStream_t)s>>>((double2 *)w, (const double2 *)h, m);
+    k_pointwise<<<grid_for(m * rows, 256), 256, 0, (cudaStream_t)s>>>((double2 *)w,
+                                                                     (const double2 *)h, m, rows);
     return (int)cudaGetLastError();
 }
 
-int tfft_bluestein_post(const void *w, const void *chirp, void *x, int64_t n, int conj_out,
-                        double scale, void *s)
+int tfft_bluestein_post(const void *w, const void *chirp, void *x, int64_t n, int64_t m,
+                        int conj_out, double scale, int64_t rows, void *s)
 {
-    k_bluestein_post<<<grid_for(n, 256), 256, 0, (cudaStream_t)s>>>(
-        (const double2 *)w, (const double2 *)chirp, (double2 *)x, n, conj_out, scale);
+    k_bluestein_post<<<grid_for(n * rows, 256), 256, 0, (cudaStream_t)s>>>(
+        (const double2 *)w, (const double2 *)chirp, (double2 *)x, n, m, conj_out, scale, rows);
     return (int)cudaGetLastError();
 }
 

@@ -167,8 +167,10 @@ int tfft_tc_error(int *flag, void *stream);
 int tfft_launch_pass(const tfft_pass *p, void *stream);
 /* can this (log_l, b_tile, arith) be launched? */
 int tfft_pass_supported(int log_l, int b_tile, int arith);
-/* out[k] = sum_j in[j] W_n^{jk} (dir 1) or conjugate kernel scaled by 1/n */
-int tfft_launch_dft(const void *in, void *out, const void *tw, int n, int dir, void *stream);
+/* out[k] = sum_j in[j] W_n^{jk} (dir 1) or conjugate kernel scaled by 1/n,
+ * for `rows` contiguous rows of n points */
+int tfft_launch_dft(const void *in, void *out, const void *tw, int n, int dir, int64_t rows,
+                    void *stream);
 /* in-place bit-reversal permutation of each line of an axis: lines are
  * (g0, g1) with strides s0, s1; element stride es; uses rev[] */
 int tfft_launch_bitrev_permute(void *data, const int *rev, int log2n, int64_t es,
@@ -178,18 +180,19 @@ int tfft_launch_bitrev_permute(void *data, const int *rev, int log2n, int64_t es
 int tfft_launch_n2(void *data, int dir, void *stream);
 
 /* Bluestein (chirp-z) pieces for a length n that is not a power of two,
- * computed through cyclic convolutions of length m >= 2n-1 (FP64):
+ * computed through cyclic convolutions of length m >= 2n-1 (FP64), for
+ * `rows` rows (x rows of n points, w rows of m points, back to back):
  *   tables: chirp[k] = exp(-pi i k^2/n), k < n; b = conj(chirp) laid out
  *           cyclically over m points (to be transformed by the caller);
  *   pre:    w = x * chirp zero-padded to m (x conjugated when conj_in);
- *   pointwise: w *= h (m points);
+ *   pointwise: w *= h (h: m points shared by every row);
  *   post:   x = w * chirp, conjugated when conj_out, times scale. */
 int tfft_bluestein_tables(void *chirp, void *b, int64_t n, int64_t m, void *stream);
 int tfft_bluestein_pre(const void *x, const void *chirp, void *w, int64_t n, int64_t m,
-                       int conj_in, void *stream);
-int tfft_pointwise(void *w, const void *h, int64_t m, void *stream);
-int tfft_bluestein_post(const void *w, const void *chirp, void *x, int64_t n, int conj_out,
-                        double scale, void *stream);
+                       int conj_in, int64_t rows, void *stream);
+int tfft_pointwise(void *w, const void *h, int64_t m, int64_t rows, void *stream);
+int tfft_bluestein_post(const void *w, const void *chirp, void *x, int64_t n, int64_t m,
+                        int conj_out, double scale, int64_t rows, void *stream);
 
 /* Real-data transforms of even length n = 2m through a complex transform of
  * length m over the same bytes (FP64):

@@ -221,7 +221,7 @@ typedef struct tope_impl {
     int oop[MAX_PASSES];
     int axis_first[3], axis_count[3];
     void *tabs[MAX_TABS];
-    int tab_key[MAX_TABS]; /* log_l * 4 + arith for W_L tables, -1 otherwise */
+    int tab_key[MAX_TABS]; /* log_l * 8 + arith for W_L tables, -1 otherwise */
     int ntabs;
     int *bitrev[3];
     void *quarter[3];
@@ -375,6 +375,9 @@ static int add_pass(struct topeFFT *f, tope_impl *P, int log_l, int64_t ies, int
     }
     int strided = (ies != 1) || (oes != 1);
     int b = (nl > 0) ? choose_b(log_l, p->n[0], strided) : 1;
+    /* few lines (small single transforms): spread them over at least 32 CTAs
+     * rather than keep wide tiles */
+    while (b > 1 && p->n[0] * p->n[1] * p->n[2] / b < 32) b >>= 1;
     if (P->arith == TFFT_ARITH_TC && log_l >= 4) {
         /* the tensor form's CTA shape is fixed per length (ragged last tile) */
         b = tfft_tc_b_tile(log_l);
@@ -424,7 +427,11 @@ static int plan_axis(struct topeFFT *f, tope_impl *P, int axis)
         }
     int st;
     const int max_lg = TFFT_MAX_LOG_L_ARITH(P->arith);
-    if (lg <= max_lg) {
+    /* a lone line of 2^10..2^13 points would be one CTA on one SM (about 70
+     * microseconds for 2^12 in FP64); two four-step passes spread it over
+     * tens of CTAs */
+    const int lone = no == 0 && lg >= 10 && P->arith != TFFT_ARITH_TC;
+    if (lg <= max_lg && !lone) {
         dimref d[4];
         memcpy(d, others, sizeof(dimref) * no);
         sort_dims(d, no);
@@ -579,7 +586,7 @@ static int impl_create(struct topeFFT *f, tope_impl **out, int ndim, int64_t x, 
     }
     if (ndim == 1 && x == 2 && batch == 1 && fp64_io && !real) P->mode = MODE_N2;
     else if (ndim == 1 && lgx < 0)
-        P->mode = !(batch == 1 && fp64_io) ? -1 : x < BLUESTEIN_MIN_N ? MODE_DFT : MODE_BLUESTEIN;
+        P->mode = !fp64_io ? -1 : x < BLUESTEIN_MIN_N ? MODE_DFT : MODE_BLUESTEIN;
     else if (lgx < 0 || lgy < 0 || lgz < 0) P->mode = -1;
     else P->mode = MODE_FFT;
     if (P->mode < 0) {
@@ -635,7 +642,7 @@ static int impl_create(struct topeFFT *f, tope_impl **out, int ndim, int64_t x, 
         while (m < 2 * x - 1) m <<= 1;
         P->bl_m = m;
         uint64_t t0 = 0, t1 = 0;
-        st = impl_create(f, &P->sub, 1, m, 1, 1, 1, NULL, P->arith, 0, &t0, &t1);
+        st = impl_create(f, &P->sub, 1, m, 1, 1, batch, NULL, P->arith, 0, &t0, &t1);
         if (!st) {
             f->live_plans--; /* the sub-plan lives and dies with this plan */
             if (tfft_malloc(&P->chirp, 16 * (size_t)x) || tfft_malloc(&P->bhat, 16 * (size_t)m))
@@ -776,22 +783,23 @@ static int impl_exec_async(struct topeFFT *f, tope_impl *P, int dir)
         if ((rc = tfft_launch_n2(P->buf[P->cur], dir, stream))) st = cuda_status(f, rc);
     } else if (P->mode == MODE_DFT) {
         rc = tfft_launch_dft(P->buf[P->cur], P->buf[1 - P->cur], P->dft_tab, (int)P->c[0], dir,
-                             stream);
+                             P->c[3], stream);
         if (rc) st = cuda_status(f, rc);
         else P->cur = 1 - P->cur;
     } else if (P->mode == MODE_BLUESTEIN) {
         /* an inverse runs as conj(F(conj x))/N around the same convolution */
         tope_impl *S = P->sub;
         const int inv = dir == INVERSE;
-        const int64_t n = P->c[0], m = P->bl_m;
-        if ((rc = tfft_bluestein_pre(P->buf[P->cur], P->chirp, S->buf[S->cur], n, m, inv, stream)))
+        const int64_t n = P->c[0], m = P->bl_m, nr = P->c[3];
+        if ((rc = tfft_bluestein_pre(P->buf[P->cur], P->chirp, S->buf[S->cur], n, m, inv, nr,
+                                     stream)))
             st = cuda_status(f, rc);
         if (!st) st = run_passes(f, S, 0, S->npass, FORWARD, 1.0);
-        if (!st && (rc = tfft_pointwise(S->buf[S->cur], P->bhat, m, stream)))
+        if (!st && (rc = tfft_pointwise(S->buf[S->cur], P->bhat, m, nr, stream)))
             st = cuda_status(f, rc);
         if (!st) st = run_passes(f, S, 0, S->npass, INVERSE, 1.0 / (double)m);
-        if (!st && (rc = tfft_bluestein_post(S->buf[S->cur], P->chirp, P->buf[P->cur], n, inv,
-                                             inv ? 1.0 / (double)n : 1.0, stream)))
+        if (!st && (rc = tfft_bluestein_post(S->buf[S->cur], P->chirp, P->buf[P->cur], n, m, inv,
+                                             inv ? 1.0 / (double)n : 1.0, nr, stream)))
             st = cuda_status(f, rc);
     }
     if (!st && P->real && dir == FORWARD) {
