@@ -66,6 +66,12 @@ WORKLOADS = {
                          "desc": "split precision: 1D C2C batched 4096 x 2^14, FP32 data, "
                                  "uniform field + Gaussian pulse 1e6 (sigma 4) per row, "
                                  "forward+inverse"},
+    "r2c_1d_2p24": {"dims": (1 << 24, 1, 1), "batch": 1, "real": True,
+                    "desc": "1D real-to-complex FP64, N=2^24 uniform[-1,1) reals, forward (R2C) "
+                            "+ inverse (C2R); GFLOP/s counts 2.5 N log2 N per direction"},
+    "1d_1e6": {"dims": (1000000, 1, 1), "batch": 1,
+               "desc": "1D C2C FP64, N=10^6 (not a power of two: Bluestein over 2^21-point "
+                       "sub-transforms), forward+inverse, uniform[-1,1) re/im"},
     "batch_uneven": {"uneven": True, "f32": False,
                      "desc": "uneven batch: 20,000 1D transforms N=2^k, k~U{6..16}, plus 500 2D "
                              "transforms with sides from {64..1024}, uniform re/im, FP64, "
@@ -143,6 +149,8 @@ def pulse_field(dims, batch, seed=SEED0 + 4, amp=1e6, sigma=4.0) -> np.ndarray:
 def make_input(wl: dict) -> np.ndarray:
     nx, ny, nz = wl["dims"]
     n = nx * ny * nz * wl["batch"]
+    if wl.get("real"):
+        return splitmix_uniform(n // 2, SEED0 + 2)  # n reals
     if wl.get("f32"):
         return pulse_field(wl["dims"], wl["batch"])
     if ny * nz > 1:
@@ -153,7 +161,24 @@ def make_input(wl: dict) -> np.ndarray:
 def flops_per_step(wl: dict) -> float:
     nx, ny, nz = wl["dims"]
     n = nx * ny * nz
-    return 2 * 5.0 * n * np.log2(n) * wl["batch"]
+    per_dir = (2.5 if wl.get("real") else 5.0) * n * np.log2(n)
+    return 2 * per_dir * wl["batch"]
+
+
+def pass_points(wl: dict) -> int:
+    """Complex points one pass launch of the dominant kernel moves: the array,
+    its packed half for real data, or the power-of-two sub-transform of a
+    Bluestein plan."""
+    nx, ny, nz = wl["dims"]
+    n = nx * ny * nz
+    if wl.get("real"):
+        return n // 2 * wl["batch"]
+    if ny * nz == 1 and n & (n - 1) and n >= 128:
+        m = 1
+        while m < 2 * n - 1:
+            m <<= 1
+        return m * wl["batch"]
+    return n * wl["batch"]
 
 
 def p_min(n: int, fp32: bool = False) -> int:
@@ -278,6 +303,29 @@ def cpu_reference_rate(wl: dict, budget_s: float = 30.0, steps: int = 1, warmup:
     nx, ny, nz = wl["dims"]
     batch = wl["batch"]
     x = make_input(wl)
+    n_all = nx * ny * nz
+    if ny * nz == 1 and n_all & (n_all - 1) and n_all >= 128:
+        # the reference's non-power-of-two path is its O(n^2) DFT kernel
+        # (kernels1D.cl:549-573): time it on a shorter length and scale by n^2
+        n_s = 20000
+        xs = x[: 2 * n_s]
+        dft = emu.dft if hasattr(emu, "dft") else emu.dft_ref
+        dft(xs, n_s)
+        t0 = time.perf_counter()
+        dft(xs, n_s)
+        t_s = time.perf_counter() - t0
+        t = 2 * t_s * (n_all / n_s) ** 2  # forward + inverse
+        gflops = flops_per_step(wl) / t / 1e9
+        sample = (f"the reference DFT (O(n^2)) at n={n_s}, forward, {t_s:.3f} s on {cores} threads, "
+                  f"scaled by (n/{n_s})^2 to n={n_all} and doubled for the inverse")
+        return gflops, {"value": round(gflops, 6), "unit": "GFLOP/s", "cores": cores,
+                        "kind": kind, "sample": sample, "ms_per_step": t * 1e3}
+    if wl.get("real"):
+        # the reference has no real-data path: its complex transform of the
+        # reals with zero imaginary parts
+        z = np.zeros(2 * n_all * batch)
+        z[0::2] = x
+        x = z
 
     def one(xs, dims, b):
         t0 = time.perf_counter()
@@ -306,7 +354,7 @@ def cpu_reference_rate(wl: dict, budget_s: float = 30.0, steps: int = 1, warmup:
             break
     t = statistics.median(times)
     n_s = sample_dims[0] * sample_dims[1] * sample_dims[2]
-    flops = 2 * 5.0 * n_s * np.log2(n_s) * sample_batch
+    flops = flops_per_step(dict(wl, dims=sample_dims, batch=sample_batch))
     gflops = flops / t / 1e9
     sample = (f"{'x'.join(map(str, sample_dims))} x batch {sample_batch}, forward+inverse, "
               f"{len(times)} timed step(s), median {t:.3f} s, {cores} threads")
@@ -328,6 +376,7 @@ def run_gpu(args, wl: dict) -> dict:
     n = nx * ny * nz
     total = n * batch
     f32 = bool(wl.get("f32"))
+    real = bool(wl.get("real"))
     es = 8 if f32 else 16
     x = make_input(wl)
     xs = x.astype(np.float32) if f32 else x  # what the plan stores
@@ -344,9 +393,9 @@ def run_gpu(args, wl: dict) -> dict:
             if single:
                 T.tope1DBatchPlanInitF32(f, p, nx, batch, T.C2C, data)
             elif batch == 1:
-                T.tope1DPlanInit(f, p, nx, T.C2C, data)
+                T.tope1DPlanInit(f, p, nx, T.R2C if real else T.C2C, data)
             else:
-                T.tope1DBatchPlanInit(f, p, nx, batch, T.C2C, data)
+                T.tope1DBatchPlanInit(f, p, nx, batch, T.R2C if real else T.C2C, data)
         elif nz == 1:
             p = T.TopePlan2D()
             (T.tope2DPlanInitF32 if single else T.tope2DPlanInit)(f, p, nx, ny, T.C2C, data)
@@ -433,7 +482,7 @@ def run_gpu(args, wl: dict) -> dict:
 
     # dominant kernel: the pass with the largest total time
     dom = max(passes, key=lambda p: p["ns"]) if passes else None
-    bytes_per_launch = 2 * es * total
+    bytes_per_launch = 2 * es * pass_points(wl)
     peak, peak_kind = measured_peaks()
     roof = None
     if dom and dom["launches"]:
@@ -450,10 +499,12 @@ def run_gpu(args, wl: dict) -> dict:
 
     # e2e through the C interface with pinned host buffers
     nbytes = xs.nbytes
-    hp = T.lib.topeHostAlloc(nbytes)
+    # a real plan's forward writes n + 2 doubles per row
+    host_vals = (n + 2) * batch if real else 2 * total
+    hp = T.lib.topeHostAlloc(host_vals * (4 if f32 else 8))
     ctype = ctypes.c_float if f32 else ctypes.c_double
-    host = np.ctypeslib.as_array((ctype * (2 * total)).from_address(hp))
-    host[:] = xs
+    host = np.ctypeslib.as_array((ctype * host_vals).from_address(hp))
+    host[:xs.size] = xs
     if f32:
         exec_fn, up_fn = T.execF32, T.uploadF32
     else:
@@ -504,13 +555,14 @@ def run_gpu(args, wl: dict) -> dict:
                                           f"129 MB L2)" if total * es > L2_BYTES else
                    "array fits in L2 (latency-bound size)",
                    "parallelism": f"replicas x{ws}"},
-        "hbm_gbs_effective": round(p_min(n, f32) * 2 * es * total * 2 / (ms * 1e-3) / 1e9, 1),
+        "hbm_gbs_effective": round((launches / args.steps) * bytes_per_launch / (ms * 1e-3) / 1e9, 1),
         "rel_l2_roundtrip": rt,
         "accuracy": accuracy,
         "roofline": roof,
         "passes": passes,
         "e2e": {"value": round(e2e_val / 1e9, 3), "unit": "GFLOP/s",
-                "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": 2 * nbytes,
+                "h2d_bytes_per_step": nbytes,
+                "d2h_bytes_per_step": (2 * nbytes + 16 * batch) if real else 2 * nbytes,
                 "ms_per_step": round(e2e_ms, 3)},
         "gpu_launches": launches,
         "clocks": clocks,
@@ -652,7 +704,8 @@ def run_batch(args, wl: dict) -> dict:
                      "bytes_per_launch": bytes_launch,
                      "launch_us": round(ms / 2 * 1e3, 1)},
         "e2e": {"value": round(e2e_val / 1e9, 3), "unit": "GFLOP/s",
-                "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": 2 * nbytes,
+                "h2d_bytes_per_step": nbytes,
+                "d2h_bytes_per_step": (2 * nbytes + 16 * batch) if real else 2 * nbytes,
                 "ms_per_step": round(e2e_ms, 3)},
         "gpu_launches": 2 * args.steps,
         "clocks": clocks,

@@ -195,7 +195,9 @@ void topeHostFree(void *p);
  * next synchronising call.  impl is a plan's t->impl. */
 void topeSetPassTiming(struct topeFFT *f, int enable);
 /* Writes up to max per-pass totals (ns) and launch counts; returns the
- * plan's number of passes. */
+ * plan's number of passes.  For a plan of a non-power-of-two length of 128
+ * points or more these are the passes of its power-of-two sub-transforms
+ * (run twice per transform), as for topePassInfo. */
 int topePassTimes(struct topeFFT *f, void *impl, uint64_t *ns, uint64_t *launches, int max);
 void topeResetPassTimes(struct topeFFT *f, void *impl);
 /* Geometry of pass i of a plan: {log2 L, lines per CTA, CTAs, threads per

@@ -1372,9 +1372,16 @@ void topeSetPassTiming(struct topeFFT *f, int enable)
     set_status(f, TOPE_SUCCESS);
 }
 
+/* the plan whose passes carry the work: a Bluestein plan's power-of-two
+ * sub-plan, otherwise the plan itself */
+static tope_impl *passes_of(tope_impl *P)
+{
+    return (P && P->mode == MODE_BLUESTEIN && P->sub) ? P->sub : P;
+}
+
 int topePassTimes(struct topeFFT *f, void *impl, uint64_t *ns, uint64_t *launches, int max)
 {
-    tope_impl *P = impl_of(f, impl);
+    tope_impl *P = passes_of(impl_of(f, impl));
     if (!P) return -1;
     int rc = tfft_stream_sync(f->command_queue);
     if (rc) {
@@ -1392,7 +1399,7 @@ int topePassTimes(struct topeFFT *f, void *impl, uint64_t *ns, uint64_t *launche
 
 void topeResetPassTimes(struct topeFFT *f, void *impl)
 {
-    tope_impl *P = impl_of(f, impl);
+    tope_impl *P = passes_of(impl_of(f, impl));
     if (!P) return;
     tfft_stream_sync(f->command_queue);
     P->pev_used = 0;
@@ -1403,7 +1410,7 @@ void topeResetPassTimes(struct topeFFT *f, void *impl)
 
 int topePassInfo(struct topeFFT *f, void *impl, int i, int64_t info[6])
 {
-    tope_impl *P = impl_of(f, impl);
+    tope_impl *P = passes_of(impl_of(f, impl));
     if (!P || !info) return -1;
     if (i < 0 || i >= P->npass) {
         set_status(f, TOPE_ERR_INVALID_ARG);
@@ -1414,7 +1421,7 @@ int topePassInfo(struct topeFFT *f, void *impl, int i, int64_t info[6])
     int64_t e = L < 16 ? L : 16;
     info[0] = p->log_l;
     info[1] = p->b_tile;
-    info[2] = (p->n[0] / p->b_tile) * p->n[1] * p->n[2];
+    info[2] = ((p->n[0] + p->b_tile - 1) / p->b_tile) * p->n[1] * p->n[2];
     info[3] = (L / e) * p->b_tile;
     info[4] = P->oop[i];
     info[5] = p->post_tw;
