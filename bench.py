@@ -764,6 +764,24 @@ def run_reference(args, wl: dict):
                     "d2h_bytes_per_step": 0}}
 
 
+def split_companion(args, wl: dict, res64: dict) -> dict:
+    """The metric sets the plain FP64 path against the split-precision form at
+    its stated error: the same workload with FP32 storage (accurate mode,
+    input with the 1e6 Gaussian pulse), its rel-L2 against the library's
+    FP64 path, and its speed-up over the FP64 line."""
+    a = argparse.Namespace(**vars(args))
+    a.split, a.no_cpu_baseline, a.steps = "accurate", True, min(args.steps, 20)
+    r = run_gpu(a, dict(wl, f32=True))
+    acc = r.get("accuracy") or {}
+    return {"mode": "accurate (FP32 data, double-float butterflies)", "value": r["value"],
+            "unit": r["unit"], "ms_per_step": r["ms_per_step"], "steps": a.steps,
+            "rel_l2_vs_fp64": acc.get("rel_l2_vs_fp64"), "max_abs_vs_fp64": acc.get("max_abs_vs_fp64"),
+            "gate": 1e-7, "speedup_vs_fp64": round(r["value"] / res64["value"], 3),
+            "roofline_frac": (r.get("roofline") or {}).get("frac"),
+            "e2e": (r.get("e2e") or {}).get("value"),
+            "input": "the same workload's uniform field plus a 1e6 Gaussian pulse, stored as FP32"}
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
@@ -775,6 +793,8 @@ def main(argv=None):
     ap.add_argument("--split", choices=sorted(SPLIT_MODES), default="accurate",
                     help="arithmetic of the FP32 (split-precision) workloads")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-split-companion", action="store_true",
+                    help="skip the split-precision run added to FP64 complex workloads")
     args = ap.parse_args(argv)
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
@@ -785,6 +805,11 @@ def main(argv=None):
         res = run_batch(args, wl)
     else:
         res = run_gpu(args, wl)
+        npts = wl["dims"][0] * wl["dims"][1] * wl["dims"][2]
+        if (res is not None and not args.no_split_companion and not wl.get("f32")
+                and not wl.get("real") and npts & (npts - 1) == 0
+                and int(os.environ.get("WORLD_SIZE", "1")) == 1):
+            res["split_precision"] = split_companion(args, wl, res)
     if res is not None:
         print(json.dumps(res), flush=True)
 
