@@ -93,6 +93,15 @@ void tope1DBatchPlanInit(struct topeFFT *f, struct topePlan1D *t, int x, int bat
  * The complex work is a transform of length x/2 on the packed reals
  * (x[2j] + i x[2j+1]) plus one pre/post pass with W_x^k twiddles. */
 void tope1DUploadSpectrum(struct topeFFT *f, struct topePlan1D *t, const double *spec);
+/* tope2DPlanInit / tope3DPlanInit with type R2C (x even, y and z powers of
+ * two): x*y(*z) reals in, x fastest; Exec(FORWARD) writes the (x/2 + 1)*y(*z)
+ * complex outputs X[kx][ky][kz], kx <= x/2, kx fastest, so d must hold
+ * (x + 2)*y(*z) doubles; Exec(INVERSE) returns the reals scaled by
+ * 1/(x*y*z).  The rows along x are a batched 1D real-data transform, then
+ * y (and z) are complex passes over the spectrum.  tope2DExecX/Y and
+ * tope3DExecX/Y/Z reject these plans (TOPE_ERR_UNSUPPORTED). */
+void tope2DUploadSpectrum(struct topeFFT *f, struct topePlan2D *t, const double *spec);
+void tope3DUploadSpectrum(struct topeFFT *f, struct topePlan3D *t, const double *spec);
 
 /* ---- split-precision form: FP32 complex data ----------------------------- */
 /* Same plans and semantics as the FP64 entry points, with interleaved FP32

@@ -121,5 +121,5 @@ def test_null_arguments_are_rejected(T):
     assert f.error == T.TOPE_ERR_INVALID_ARG
     T.tope2DPlanInit(f, t, 6, 4, T.C2C, np.zeros(48))
     assert f.error == T.TOPE_ERR_INVALID_SIZE
-    T.tope2DPlanInit(f, t, 4, 4, T.R2C, np.zeros(32))
+    T.tope2DPlanInit(f, t, 4, 4, 5, np.zeros(32))  # neither C2C nor R2C
     assert f.error == T.TOPE_ERR_UNSUPPORTED

@@ -104,12 +104,86 @@ def test_r2c_device_resident_chain(T, fw, orc):
     T.tope1DDestroy(fw, t)
 
 
-def test_r2c_rejects_odd_and_split_precision(T, fw):
+def test_r2c_rejects_bad_shapes_and_split_precision(T, fw):
     t = T.TopePlan1D()
     T.tope1DPlanInit(fw, t, 7, T.R2C, np.zeros(16))
     assert fw.error == T.TOPE_ERR_INVALID_SIZE and not t.impl
     T.tope1DBatchPlanInitF32(fw, t, 64, 1, T.R2C, np.zeros(130, dtype=np.float32))
     assert fw.error == T.TOPE_ERR_UNSUPPORTED and not t.impl
     t2 = T.TopePlan2D()
-    T.tope2DPlanInit(fw, t2, 8, 8, T.R2C, np.zeros(128))
-    assert fw.error == T.TOPE_ERR_UNSUPPORTED and not t2.impl
+    T.tope2DPlanInit(fw, t2, 7, 8, T.R2C, np.zeros(128))  # odd x
+    assert fw.error == T.TOPE_ERR_INVALID_SIZE and not t2.impl
+    T.tope2DPlanInit(fw, t2, 8, 6, T.R2C, np.zeros(128))  # y not a power of two
+    assert fw.error == T.TOPE_ERR_INVALID_SIZE and not t2.impl
+
+
+# ---------------------------------------------------------------- 2D / 3D
+def oracle_spectrum_nd(orc, xr, dims):
+    """X[kz][ky][kx], kx <= nx/2, kx fastest, long double, from the
+    complexified reals."""
+    nx, ny, nz = dims
+    z = np.zeros(2 * nx * ny * nz)
+    z[0::2] = xr
+    zz = orc.fft_ld(z, nx, ny, nz, dir_=1).reshape(nz, ny, nx, 2)
+    return np.ascontiguousarray(zz[:, :, : nx // 2 + 1, :]).ravel()
+
+
+def make_plan_nd(T, f, dims, d):
+    nx, ny, nz = dims
+    if nz == 1:
+        t = T.TopePlan2D()
+        T.tope2DPlanInit(f, t, nx, ny, T.R2C, d)
+    else:
+        t = T.TopePlan3D()
+        T.tope3DPlanInit(f, t, nx, ny, nz, T.R2C, d)
+    T.check(f)
+    return t
+
+
+def destroy_nd(T, f, t):
+    (T.tope2DDestroy if isinstance(t, T.TopePlan2D) else T.tope3DDestroy)(f, t)
+    T.check(f)
+
+
+ND = [(8, 4, 1), (64, 32, 1), (512, 256, 1), (4096, 4096, 1), (2, 2, 1), (16, 8, 4),
+      (64, 32, 16), (256, 256, 256), (32, 1 << 14, 1)]
+
+
+@pytest.mark.parametrize("dims", ND, ids=lambda d: "x".join(map(str, d)))
+def test_r2c_nd_forward_and_round_trip(T, fw, orc, dims):
+    nx, ny, nz = dims
+    n = nx * ny * nz
+    xr = orc.uniform(n // 2, SEED0 + 5 * nx + ny)
+    d = np.zeros((nx + 2) * ny * nz)
+    d[:n] = xr
+    t = make_plan_nd(T, fw, dims, d)
+    exec_fn = T.tope2DExec if nz == 1 else T.tope3DExec
+    exec_fn(fw, t, d, T.FORWARD)
+    T.check(fw)
+    tol = 1e-13 * max(1.0, np.log2(n))
+    if n <= 1 << 20:
+        assert orc.rel_l2(d, oracle_spectrum_nd(orc, xr, dims)) <= tol
+    back = np.zeros((nx + 2) * ny * nz)
+    exec_fn(fw, t, back, T.INVERSE)
+    T.check(fw)
+    assert orc.rel_l2(back[:n], xr) <= tol
+    destroy_nd(T, fw, t)
+
+
+@pytest.mark.parametrize("dims", [(64, 32, 1), (16, 8, 4)], ids=lambda d: "x".join(map(str, d)))
+def test_c2r_nd_from_uploaded_spectrum(T, fw, orc, dims):
+    nx, ny, nz = dims
+    n = nx * ny * nz
+    xr = orc.uniform(n // 2, SEED0 + 13)
+    t = make_plan_nd(T, fw, dims, np.zeros(n))
+    T.upload_spectrum(fw, t, oracle_spectrum_nd(orc, xr, dims))
+    T.check(fw)
+    out = np.zeros((nx + 2) * ny * nz)
+    (T.tope2DExec if nz == 1 else T.tope3DExec)(fw, t, out, T.INVERSE)
+    T.check(fw)
+    assert orc.rel_l2(out[:n], xr) <= 1e-13 * np.log2(n)
+    # single-axis execution is for complex plans only
+    if nz == 1:
+        T.tope2DExecX(fw, t)
+        assert fw.error == T.TOPE_ERR_UNSUPPORTED
+    destroy_nd(T, fw, t)

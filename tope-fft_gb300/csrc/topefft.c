@@ -238,6 +238,9 @@ typedef struct tope_impl {
     void *rtw_hi, *rtw_lo;
     int rtw_shift;
     int spec_cur; /* the spectrum, not the real array, is the current data */
+    /* 2D/3D real-data plan: the C2C plan over the spectrum's y (and z) axes,
+     * whose buffer holds the spectrum (x/2 + 1 points per row) */
+    struct tope_impl *specp;
     tope_evpair kev, mev;
     int pending;         /* kev recorded by an async exec, not yet accounted */
     int last_dir;
@@ -316,7 +319,12 @@ static int choose_b(int log_l, int64_t n0, int strided)
     if (maxb > 32) maxb = 32;
     if (want > maxb) want = maxb;
     if (want < 1) want = 1;
-    return pow2_divisor(n0, (int)want);
+    /* a line count with no large power-of-two divisor (a real plan's
+     * spectrum width x/2 + 1, odd batch counts) takes full tiles and one
+     * ragged last tile rather than narrow tiles */
+    int b = pow2_divisor(n0, (int)want);
+    if (b < want && n0 > want) b = (int)want;
+    return b;
 }
 
 typedef struct dimref {
@@ -483,6 +491,7 @@ static void impl_free(tope_impl *P)
     tfft_free(P->spec);
     tfft_free(P->rtw_hi);
     tfft_free(P->rtw_lo);
+    impl_free(P->specp);
     impl_free(P->sub);
     tfft_free(P->buf[0]);
     tfft_free(P->buf[1]);
@@ -535,10 +544,14 @@ static void pev_settle(tope_impl *P)
 static int run_passes(struct topeFFT *f, tope_impl *P, int first, int count, int dir,
                       double scale);
 
+/* kinds of impl_create's `real` argument */
+#define IMPL_REAL 1 /* rows of a real-data plan: x complex points carry 2x reals */
+#define IMPL_SPEC 2 /* the spectrum of a 2D/3D real-data plan: only y and z are
+                       transformed, x (= half length + 1) is a line count */
+
 /* Build the device state of a plan and upload d (complex elements of the
  * arithmetic's storage type; arith < 0 takes the framework's setting).
- * real: a 1D real-data plan of length 2x (x complex points carry the packed
- * reals; FP64 storage only).  Returns a status. */
+ * real: 0, IMPL_REAL or IMPL_SPEC (FP64 storage only).  Returns a status. */
 static int impl_create(struct topeFFT *f, tope_impl **out, int ndim, int64_t x, int64_t y,
                        int64_t z, int64_t batch, const void *d, int arith, int real,
                        uint64_t *t_pre, uint64_t *t_mem)
@@ -579,12 +592,14 @@ static int impl_create(struct topeFFT *f, tope_impl **out, int ndim, int64_t x, 
 
     int lgx = ilog2_exact64(x), lgy = ilog2_exact64(y), lgz = ilog2_exact64(z);
     const int fp64_io = P->es == 16;
-    P->real = real;
-    if (real && (ndim != 1 || !fp64_io)) {
+    P->real = real == IMPL_REAL;
+    const int spec = real == IMPL_SPEC;
+    if ((P->real && ndim != 1) || (real && !fp64_io)) {
         impl_free(P);
         return set_status(f, TOPE_ERR_UNSUPPORTED);
     }
-    if (ndim == 1 && x == 2 && batch == 1 && fp64_io && !real) P->mode = MODE_N2;
+    if (spec) P->mode = (lgy < 0 || lgz < 0) ? -1 : MODE_FFT;
+    else if (ndim == 1 && x == 2 && batch == 1 && fp64_io && !real) P->mode = MODE_N2;
     else if (ndim == 1 && lgx < 0)
         P->mode = !fp64_io ? -1 : x < BLUESTEIN_MIN_N ? MODE_DFT : MODE_BLUESTEIN;
     else if (lgx < 0 || lgy < 0 || lgz < 0) P->mode = -1;
@@ -610,12 +625,12 @@ static int impl_create(struct topeFFT *f, tope_impl **out, int ndim, int64_t x, 
             if (tfft_malloc(&P->tc_matrix, TFFT_TC_MATRIX_BYTES)) st = set_status(f, TOPE_ERR_ALLOC);
             else if ((rc = tfft_tc_matrix(P->tc_matrix, stream))) st = cuda_status(f, rc);
         }
-        for (int a = 0; a < 3 && !st; a++) st = plan_axis(f, P, a);
+        for (int a = spec ? 1 : 0; a < 3 && !st; a++) st = plan_axis(f, P, a);
         int need2 = 0;
         for (int i = 0; i < P->npass; i++) need2 |= P->oop[i];
         if (!st && need2 && tfft_malloc(&P->buf[1], bytes)) st = set_status(f, TOPE_ERR_ALLOC);
         /* per-axis bit-reversal and quarter-wave tables of the reference's plan */
-        for (int a = 0; a < ndim && !st; a++) {
+        for (int a = spec ? 1 : 0; a < ndim && !st; a++) {
             int lg = ilog2_exact64(P->c[a]);
             if (tfft_malloc((void **)&P->bitrev[a], sizeof(int) * (size_t)P->c[a])) {
                 st = set_status(f, TOPE_ERR_ALLOC);
@@ -661,7 +676,7 @@ static int impl_create(struct topeFFT *f, tope_impl **out, int ndim, int64_t x, 
         else if ((rc = tfft_bitrev_table(P->bitrev[0], 1, stream)))
             st = cuda_status(f, rc);
     }
-    if (!st && real) {
+    if (!st && P->real) {
         /* spectrum rows of x + 1 points; W_{2x}^k from two tables of about
          * sqrt(2x) entries each */
         int shift = 0;
@@ -752,6 +767,13 @@ static int run_passes(struct topeFFT *f, tope_impl *P, int first, int count, int
     return TOPE_SUCCESS;
 }
 
+/* where a real-data plan's spectrum lives: its own buffer (1D) or the
+ * current buffer of its spectrum plan (2D/3D) */
+static void *spec_buf(const tope_impl *P)
+{
+    return P->specp ? P->specp->buf[P->specp->cur] : P->spec;
+}
+
 /* queue the whole transform; events bracket the kernels */
 static int impl_exec_async(struct topeFFT *f, tope_impl *P, int dir)
 {
@@ -764,9 +786,14 @@ static int impl_exec_async(struct topeFFT *f, tope_impl *P, int dir)
     tfft_event_record(w->pair.a, stream);
     const int64_t rows = P->c[3], m = P->c[0];
     if (P->real && dir == INVERSE) {
+        /* 2D/3D: the inverse along y (and z) on the spectrum first */
+        if (P->specp) {
+            tope_impl *Q = P->specp;
+            st = run_passes(f, Q, 0, Q->npass, INVERSE, 1.0 / (double)(Q->c[1] * Q->c[2]));
+        }
         /* spectrum -> packed spectrum of the half-length transform */
-        if ((rc = tfft_c2r_pre(P->spec, P->buf[P->cur], P->rtw_hi, P->rtw_lo, P->rtw_shift, m,
-                               rows, stream)))
+        if (!st && (rc = tfft_c2r_pre(spec_buf(P), P->buf[P->cur], P->rtw_hi, P->rtw_lo,
+                                      P->rtw_shift, m, rows, stream)))
             st = cuda_status(f, rc);
         P->spec_cur = 0;
     }
@@ -803,9 +830,11 @@ static int impl_exec_async(struct topeFFT *f, tope_impl *P, int dir)
             st = cuda_status(f, rc);
     }
     if (!st && P->real && dir == FORWARD) {
-        if ((rc = tfft_r2c_post(P->buf[P->cur], P->spec, P->rtw_hi, P->rtw_lo, P->rtw_shift, m,
-                                rows, stream)))
+        if ((rc = tfft_r2c_post(P->buf[P->cur], spec_buf(P), P->rtw_hi, P->rtw_lo, P->rtw_shift,
+                                m, rows, stream)))
             st = cuda_status(f, rc);
+        /* 2D/3D: then the forward along y (and z) on the spectrum */
+        if (!st && P->specp) st = run_passes(f, P->specp, 0, P->specp->npass, FORWARD, 1.0);
         P->spec_cur = 1;
     }
     tfft_event_record(P->kev.b, stream);
@@ -819,7 +848,7 @@ static void *cur_data(const tope_impl *P, size_t *bytes)
 {
     if (P->real && P->spec_cur) {
         *bytes = (size_t)16 * (size_t)(P->c[0] + 1) * (size_t)P->c[3];
-        return P->spec;
+        return spec_buf(P);
     }
     *bytes = (size_t)P->total * P->es;
     return P->buf[P->cur];
@@ -872,6 +901,7 @@ static int impl_exec(struct topeFFT *f, tope_impl *P, void *d, int es_caller, in
 
 static int impl_axis(struct topeFFT *f, tope_impl *P, int axis, uint64_t *t_kernel)
 {
+    if (P->real) return set_status(f, TOPE_ERR_UNSUPPORTED); /* whole transforms only */
     if (axis >= P->ndim || P->mode != MODE_FFT) return set_status(f, TOPE_ERR_INVALID_ARG);
     void *stream = f->command_queue;
     tfft_event_record(P->kev.a, stream);
@@ -1032,17 +1062,17 @@ void tope1DDownload(struct topeFFT *f, struct topePlan1D *t, double *d)
     if (P) impl_download(f, P, d, 16, &t->totalKernel, &t->totalMemory);
 }
 
-void tope1DUploadSpectrum(struct topeFFT *f, struct topePlan1D *t, const double *spec)
+static void impl_upload_spectrum(struct topeFFT *f, tope_impl *P, const double *spec,
+                                 uint64_t *t_mem)
 {
-    tope_impl *P = t ? impl_of(f, t->impl) : NULL;
-    if (!P) return;
     if (!P->real || !spec) {
         set_status(f, TOPE_ERR_INVALID_ARG);
         return;
     }
     void *stream = f->command_queue;
     tfft_event_record(P->mev.a, stream);
-    int rc = tfft_h2d(P->spec, spec, (size_t)16 * (size_t)(P->c[0] + 1) * (size_t)P->c[3], stream);
+    int rc = tfft_h2d(spec_buf(P), spec, (size_t)16 * (size_t)(P->c[0] + 1) * (size_t)P->c[3],
+                      stream);
     tfft_event_record(P->mev.b, stream);
     if (!rc) rc = tfft_stream_sync(stream);
     if (rc) {
@@ -1052,8 +1082,26 @@ void tope1DUploadSpectrum(struct topeFFT *f, struct topePlan1D *t, const double 
     P->spec_cur = 1;
     uint64_t ns = 0;
     tfft_event_elapsed_ns(P->mev.a, P->mev.b, &ns);
-    t->totalMemory += ns;
+    *t_mem += ns;
     set_status(f, TOPE_SUCCESS);
+}
+
+void tope1DUploadSpectrum(struct topeFFT *f, struct topePlan1D *t, const double *spec)
+{
+    tope_impl *P = t ? impl_of(f, t->impl) : NULL;
+    if (P) impl_upload_spectrum(f, P, spec, &t->totalMemory);
+}
+
+void tope2DUploadSpectrum(struct topeFFT *f, struct topePlan2D *t, const double *spec)
+{
+    tope_impl *P = t ? impl_of(f, t->impl) : NULL;
+    if (P) impl_upload_spectrum(f, P, spec, &t->totalMemory);
+}
+
+void tope3DUploadSpectrum(struct topeFFT *f, struct topePlan3D *t, const double *spec)
+{
+    tope_impl *P = t ? impl_of(f, t->impl) : NULL;
+    if (P) impl_upload_spectrum(f, P, spec, &t->totalMemory);
 }
 
 void tope1DDestroy(struct topeFFT *f, struct topePlan1D *t)
@@ -1068,6 +1116,32 @@ void tope1DDestroy(struct topeFFT *f, struct topePlan1D *t)
 /* ------------------------------------------------------------------------ */
 /* public: 2D                                                               */
 /* ------------------------------------------------------------------------ */
+/* A 2D/3D real-data plan of x * y * z reals (x even, y and z powers of two):
+ * the rows along x as a batched 1D real-data plan of y*z rows, whose
+ * spectrum (x/2 + 1 points per row) is the buffer of a second plan that
+ * transforms along y and z only. */
+static int real_nd_create(struct topeFFT *f, tope_impl **out, int ndim, int64_t x, int64_t y,
+                          int64_t z, const void *d, int arith, uint64_t *t_pre, uint64_t *t_mem)
+{
+    *out = NULL;
+    if (x < 2 || x % 2 || ilog2_exact64(y) < 0 || ilog2_exact64(z) < 0)
+        return set_status(f, TOPE_ERR_INVALID_SIZE);
+    tope_impl *P, *Q;
+    int st = impl_create(f, &P, 1, x / 2, 1, 1, y * z, d, arith, IMPL_REAL, t_pre, t_mem);
+    if (st) return st;
+    st = impl_create(f, &Q, ndim, x / 2 + 1, y, z, 1, NULL, P->arith, IMPL_SPEC, t_pre, t_mem);
+    if (st) {
+        impl_destroy(f, P);
+        return set_status(f, st);
+    }
+    f->live_plans--; /* the spectrum plan lives and dies with P */
+    P->specp = Q;
+    tfft_free(P->spec); /* the spectrum lives in Q's buffer */
+    P->spec = NULL;
+    *out = P;
+    return set_status(f, TOPE_SUCCESS);
+}
+
 static void plan2d(struct topeFFT *f, struct topePlan2D *t, int x, int y, int type,
                    const void *d, int arith)
 {
@@ -1080,6 +1154,15 @@ static void plan2d(struct topeFFT *f, struct topePlan2D *t, int x, int y, int ty
     t->y = y;
     t->type = type;
     t->dim = 2;
+    if (type == R2C) {
+        tope_impl *P;
+        if (real_nd_create(f, &P, 2, x, y, 1, d, arith, &t->totalPreKernel, &t->totalMemory))
+            return;
+        t->impl = P;
+        t->dataSize = (size_t)8 * (size_t)x * (size_t)y;
+        t->data = P->buf[P->cur];
+        return;
+    }
     if (type != C2C) {
         set_status(f, TOPE_ERR_UNSUPPORTED);
         return;
@@ -1192,6 +1275,15 @@ static void plan3d(struct topeFFT *f, struct topePlan3D *t, int x, int y, int z,
     t->z = z;
     t->type = type;
     t->dim = 3;
+    if (type == R2C) {
+        tope_impl *P;
+        if (real_nd_create(f, &P, 3, x, y, z, d, arith, &t->totalPreKernel, &t->totalMemory))
+            return;
+        t->impl = P;
+        t->dataSize = (size_t)8 * (size_t)x * (size_t)y * (size_t)z;
+        t->data = P->buf[P->cur];
+        return;
+    }
     if (type != C2C) {
         set_status(f, TOPE_ERR_UNSUPPORTED);
         return;

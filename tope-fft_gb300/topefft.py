@@ -128,6 +128,8 @@ SIGNATURES = [
     ("tope1DUpload", None, [_F, _P1, _D]),
     ("tope1DDownload", None, [_F, _P1, _D]),
     ("tope1DUploadSpectrum", None, [_F, _P1, _D]),
+    ("tope2DUploadSpectrum", None, [_F, _P2, _D]),
+    ("tope3DUploadSpectrum", None, [_F, _P3, _D]),
     ("tope2DUpload", None, [_F, _P2, _D]),
     ("tope2DDownload", None, [_F, _P2, _D]),
     ("tope3DUpload", None, [_F, _P3, _D]),
@@ -299,7 +301,9 @@ def download(f, t, d) -> None:
 
 def upload_spectrum(f, t, spec) -> None:
     """R2C plans: the x/2 + 1 complex outputs per row, for an inverse."""
-    lib.tope1DUploadSpectrum(C.byref(f), C.byref(t), _ptr(spec))
+    fn = {TopePlan1D: lib.tope1DUploadSpectrum, TopePlan2D: lib.tope2DUploadSpectrum,
+          TopePlan3D: lib.tope3DUploadSpectrum}[type(t)]
+    fn(C.byref(f), C.byref(t), _ptr(spec))
 
 
 def topeSync(f) -> None:
