@@ -15,9 +15,11 @@ static int ilog2_exact(int v)
     return (1 << l) == v ? l : -1;
 }
 
-static LaunchFn find(int log_l, int b_tile, int arith)
+static LaunchFn find(int log_l, int b_tile, int arith, int ept)
 {
     const int log_b = ilog2_exact(b_tile);
+    if (ept == 4) return log_b < 0 ? nullptr : launcher_small(arith, log_l, log_b);
+    if (ept != 0 && ept != 16) return nullptr;
     /* the tensor form fixes its lines per CTA (up to 256 for L = 16) */
     if (arith == TFFT_ARITH_TC && log_l >= 4)
         return log_l <= 13 && b_tile == tfft_tc_b_tile(log_l) ? launcher_tc(log_l) : nullptr;
@@ -48,14 +50,14 @@ static LaunchFn find(int log_l, int b_tile, int arith)
 
 } // namespace tfft
 
-extern "C" int tfft_pass_supported(int log_l, int b_tile, int arith)
+extern "C" int tfft_pass_supported(int log_l, int b_tile, int arith, int ept)
 {
-    return tfft::find(log_l, b_tile, arith) != nullptr;
+    return tfft::find(log_l, b_tile, arith, ept) != nullptr;
 }
 
 extern "C" int tfft_launch_pass(const tfft_pass *p, void *stream)
 {
-    tfft::LaunchFn f = tfft::find(p->log_l, p->b_tile, p->arith);
+    tfft::LaunchFn f = tfft::find(p->log_l, p->b_tile, p->arith, p->ept);
     if (!f) return (int)cudaErrorInvalidValue;
     return f(*p, (cudaStream_t)stream);
 }

@@ -134,20 +134,26 @@ __device__ __forceinline__ unsigned tile_max_exp(const double2 (&raw)[E])
 template <int B>
 __device__ __forceinline__ int sidx(int p, int b) { return (p + (p >> 4)) * B + b; }
 
-template <int LOG_L>
+/* Stage structure of a line of 2^LOG_L points, EPT (16 or 4) points per
+ * thread: an optional first stage of radix 2^(LOG_L mod log2 EPT), then
+ * stages of radix EPT.  EPT = 4 serves small single transforms, where more
+ * threads per point shorten each thread's chain of dependent instructions. */
+template <int LOG_L, int EPT = 16>
 struct Shape {
+    static constexpr int LE = EPT == 16 ? 4 : 2;   /* log2 of the main radix */
     static constexpr int L = 1 << LOG_L;
-    static constexpr int E = L < 16 ? L : 16;      /* points per thread */
+    static constexpr int E = L < EPT ? L : EPT;    /* points per thread */
     static constexpr int TPL = L / E;              /* threads per line */
-    static constexpr int LR0 = LOG_L <= 4 ? LOG_L : (LOG_L % 4);
+    static constexpr int LR0 = LOG_L <= LE ? LOG_L : (LOG_L % LE);
     static constexpr int R0 = 1 << LR0;            /* first-stage radix */
-    static constexpr int NSTAGE = LOG_L <= 4 ? 1 : (LR0 ? 1 : 0) + LOG_L / 4;
+    static constexpr int NSTAGE = LOG_L <= LE ? 1 : (LR0 ? 1 : 0) + LOG_L / LE;
+    static_assert(EPT == 16 || EPT == 4, "16 or 4 points per thread");
 };
 
-template <class A, int LOG_L, int B>
+template <class A, int LOG_L, int B, int EPT = 16>
 __host__ __device__ constexpr size_t pass_smem_bytes()
 {
-    return Shape<LOG_L>::TPL > 1
+    return Shape<LOG_L, EPT>::TPL > 1
                ? (size_t)((1 << LOG_L) + ((1 << LOG_L) >> 4)) * B * sizeof(typename A::S)
                : 0;
 }
@@ -158,12 +164,12 @@ __host__ __device__ constexpr size_t pass_smem_bytes()
  * registers then already hold the loaded points); writes to shared memory
  * unless it is the last stage (the registers then hold natural-order output).
  */
-template <class A, int LOG_L, int B, int R, int NS, bool FROM_SMEM, bool TO_SMEM>
+template <class A, int LOG_L, int B, int R, int NS, bool FROM_SMEM, bool TO_SMEM, int EPT = 16>
 __device__ __forceinline__ void stage(typename A::C *a, typename A::S *sm, int j, int b,
                                       const void *tw)
 {
     using C = typename A::C;
-    using SH = Shape<LOG_L>;
+    using SH = Shape<LOG_L, EPT>;
     constexpr int L = SH::L, E = SH::E, TPL = SH::TPL;
     if constexpr (FROM_SMEM) {
 #pragma unroll
@@ -198,44 +204,44 @@ __device__ __forceinline__ void stage(typename A::C *a, typename A::S *sm, int j
     }
 }
 
-/* stages after the first: radix 16, Ns = R0 * 16^s */
-template <class A, int LOG_L, int B, int S>
+/* stages after the first: radix EPT, Ns = R0 * EPT^(s-1) */
+template <class A, int LOG_L, int B, int S, int EPT = 16>
 __device__ __forceinline__ void stages16(typename A::C *a, typename A::S *sm, int j, int b,
                                          const void *tw)
 {
-    using SH = Shape<LOG_L>;
+    using SH = Shape<LOG_L, EPT>;
     if constexpr (S < SH::NSTAGE) {
-        constexpr int first_log = SH::LR0 ? SH::LR0 : 4;
-        constexpr int NS = 1 << (first_log + 4 * (S - 1));
+        constexpr int first_log = SH::LR0 ? SH::LR0 : SH::LE;
+        constexpr int NS = 1 << (first_log + SH::LE * (S - 1));
         constexpr bool last = (S == SH::NSTAGE - 1);
-        stage<A, LOG_L, B, 16, NS, true, !last>(a, sm, j, b, tw);
-        stages16<A, LOG_L, B, S + 1>(a, sm, j, b, tw);
+        stage<A, LOG_L, B, EPT, NS, true, !last, EPT>(a, sm, j, b, tw);
+        stages16<A, LOG_L, B, S + 1, EPT>(a, sm, j, b, tw);
     }
 }
 
-template <class A, int LOG_L, int B>
+template <class A, int LOG_L, int B, int EPT = 16>
 __device__ __forceinline__ void fft_line_regs(typename A::C *a, typename A::S *sm, int j, int b,
                                               const void *tw)
 {
-    using SH = Shape<LOG_L>;
+    using SH = Shape<LOG_L, EPT>;
     if constexpr (LOG_L == 0) {
         return;
     } else if constexpr (SH::NSTAGE == 1) {
-        stage<A, LOG_L, B, SH::R0, 1, false, false>(a, sm, j, b, tw);
+        stage<A, LOG_L, B, SH::R0, 1, false, false, EPT>(a, sm, j, b, tw);
     } else {
-        constexpr int R_first = SH::LR0 ? SH::R0 : 16;
-        stage<A, LOG_L, B, R_first, 1, false, true>(a, sm, j, b, tw);
-        stages16<A, LOG_L, B, 1>(a, sm, j, b, tw);
+        constexpr int R_first = SH::LR0 ? SH::R0 : EPT;
+        stage<A, LOG_L, B, R_first, 1, false, true, EPT>(a, sm, j, b, tw);
+        stages16<A, LOG_L, B, 1, EPT>(a, sm, j, b, tw);
     }
 }
 
 /* the in-register line transform of run_tile: all stages on the CUDA cores */
 struct CoreLine {
-    template <class A, int LOG_L, int B>
+    template <class A, int LOG_L, int B, int EPT = 16>
     __device__ __forceinline__ void run(typename A::C *a, typename A::S *sm, int j, int b,
                                         const tfft_pass &p)
     {
-        fft_line_regs<A, LOG_L, B>(a, sm, j, b, p.tw);
+        fft_line_regs<A, LOG_L, B, EPT>(a, sm, j, b, p.tw);
     }
 };
 
@@ -276,13 +282,13 @@ __device__ __forceinline__ TileGeom tile_geom(const tfft_pass &p, int64_t tile, 
 /* Everything after the loads: the tile scaling of the double-float FP64
  * arithmetic, conjugation, the line transform, the four-step twiddle, and
  * the store (conjugation and scale fused) */
-template <class A, int LOG_L, int B, class LINE>
+template <class A, int LOG_L, int B, class LINE, int EPT = 16>
 __device__ __forceinline__ void finish_tile(const tfft_pass &p, const TileGeom &g,
-                                            typename A::Store (&raw)[Shape<LOG_L>::E],
+                                            typename A::Store (&raw)[Shape<LOG_L, EPT>::E],
                                             typename A::S *sm, int j, int b, LINE &line)
 {
     using C = typename A::C;
-    using SH = Shape<LOG_L>;
+    using SH = Shape<LOG_L, EPT>;
     using Store = typename A::Store;
     constexpr int E = SH::E, TPL = SH::TPL;
     /* arithmetics with a narrower exponent range than their storage work on
@@ -310,7 +316,7 @@ __device__ __forceinline__ void finish_tile(const tfft_pass &p, const TileGeom &
         a[q] = p.conj_in ? A::conj(v) : v;
     }
 
-    line.template run<A, LOG_L, B>(a, sm, j, b, p);
+    line.template run<A, LOG_L, B, EPT>(a, sm, j, b, p);
 
     if (p.post_tw) {
         const int64_t t = p.tw_level == 0 ? g.g0 : g.g1;
@@ -341,11 +347,11 @@ __device__ __forceinline__ void finish_tile(const tfft_pass &p, const TileGeom &
  * streaming hint.  LINE transforms the loaded points (CoreLine, or the
  * tensor-core stages of fft_tc.cuh).
  */
-template <class A, int LOG_L, int B, bool L2ONLY, class LINE = CoreLine>
+template <class A, int LOG_L, int B, bool L2ONLY, class LINE = CoreLine, int EPT = 16>
 __device__ __forceinline__ void run_tile(const tfft_pass &p, int64_t tile, unsigned char *smem_raw,
                                          LINE line = LINE{})
 {
-    using SH = Shape<LOG_L>;
+    using SH = Shape<LOG_L, EPT>;
     using Store = typename A::Store;
     constexpr int E = SH::E, TPL = SH::TPL;
     typename A::S *sm = reinterpret_cast<typename A::S *>(smem_raw);
@@ -361,7 +367,7 @@ __device__ __forceinline__ void run_tile(const tfft_pass &p, int64_t tile, unsig
             raw[q] = __ldcs(in + (int64_t)(j + q * TPL) * p.ies);
         }
     }
-    finish_tile<A, LOG_L, B>(p, g, raw, sm, j, b, line);
+    finish_tile<A, LOG_L, B, LINE, EPT>(p, g, raw, sm, j, b, line);
 }
 
 /* Minimum CTAs per SM in the launch bounds.  0 leaves the register count to
@@ -376,22 +382,22 @@ constexpr int pass_min_blocks()
     return A::kScaled && W < 16 ? 16 / W : 0;
 }
 
-template <class A, int LOG_L, int B>
+template <class A, int LOG_L, int B, int EPT = 16>
 __global__ void
-__launch_bounds__(Shape<LOG_L>::TPL * B, pass_min_blocks<A, Shape<LOG_L>::TPL * B>())
+__launch_bounds__(Shape<LOG_L, EPT>::TPL * B, pass_min_blocks<A, Shape<LOG_L, EPT>::TPL * B>())
     pass_kernel(const tfft_pass p)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    run_tile<A, LOG_L, B, false>(p, blockIdx.x, smem_raw);
+    run_tile<A, LOG_L, B, false, CoreLine, EPT>(p, blockIdx.x, smem_raw);
 }
 
-template <class A, int LOG_L, int LOG_B>
+template <class A, int LOG_L, int LOG_B, int EPT = 16>
 int launch_pass(const tfft_pass &p, cudaStream_t s)
 {
     constexpr int B = 1 << LOG_B;
-    constexpr size_t smem = pass_smem_bytes<A, LOG_L, B>();
+    constexpr size_t smem = pass_smem_bytes<A, LOG_L, B, EPT>();
     static unsigned attr_done = 0; /* one bit per device ordinal */
-    auto kern = pass_kernel<A, LOG_L, B>;
+    auto kern = pass_kernel<A, LOG_L, B, EPT>;
     if constexpr (smem > 48 * 1024) {
         int dev = 0;
         cudaGetDevice(&dev);
@@ -405,7 +411,7 @@ int launch_pass(const tfft_pass &p, cudaStream_t s)
     }
     const int64_t blocks = ((p.n[0] + B - 1) / B) * p.n[1] * p.n[2];
     if (blocks <= 0) return 0;
-    kern<<<(unsigned)blocks, Shape<LOG_L>::TPL * B, smem, s>>>(p);
+    kern<<<(unsigned)blocks, Shape<LOG_L, EPT>::TPL * B, smem, s>>>(p);
     return (int)cudaGetLastError();
 }
 
@@ -486,6 +492,9 @@ LaunchFn launcher_df32_4(int log_l, int log_b);
 LaunchFn launcher_df32_5(int log_l, int log_b);
 /* tensor form (fft_inst_tc.cu): one lines-per-CTA value per log2 L */
 LaunchFn launcher_tc(int log_l);
+/* 4 points per thread (fft_inst_small.cu): FP64-storage arithmetics,
+ * log2 L = 2..7, log2 L + log2 B <= 12 */
+LaunchFn launcher_small(int arith, int log_l, int log_b);
 
 } // namespace tfft
 

@@ -280,9 +280,10 @@ __device__ __forceinline__ void stages(float2 *a, float2 *sm, int j, int b, cons
 /* run_tile's line transform for the tensor form (one tile per CTA) */
 struct Line {
     Ctx cx;
-    template <class A, int LOG_L, int B>
+    template <class A, int LOG_L, int B, int EPT = 16>
     __device__ __forceinline__ void run(float2 *a, float2 *sm, int j, int b, const tfft_pass &p)
     {
+        static_assert(EPT == 16, "the tensor stages hold 16 points per thread");
         static_assert(LOG_L >= 4, "a radix-16 stage needs 16 points");
         using SH = Shape<LOG_L>;
         if constexpr (SH::LR0) {

@@ -75,6 +75,9 @@ typedef struct tfft_pass {
     /* TFFT_ARITH_TC: the 3 BF16 pieces of the real 32x32 DFT-16 matrix in
      * the tensor cores' shared-memory layout (tfft_tc_matrix) */
     const void *mma_b;
+    /* points per thread: 0 or 16 (radix-16 stages), or 4 (radix-4 stages,
+     * FP64 storage, log2 L = 2..7: small transforms) */
+    int ept;
 } tfft_pass;
 
 /* ---- batches of independent transforms (persistent kernel) --------------- */
@@ -165,8 +168,8 @@ int tfft_tc_error(int *flag, void *stream);
 
 /* ---- kernels -------------------------------------------------------------- */
 int tfft_launch_pass(const tfft_pass *p, void *stream);
-/* can this (log_l, b_tile, arith) be launched? */
-int tfft_pass_supported(int log_l, int b_tile, int arith);
+/* can this (log_l, b_tile, arith, points per thread) be launched? */
+int tfft_pass_supported(int log_l, int b_tile, int arith, int ept);
 /* out[k] = sum_j in[j] W_n^{jk} (dir 1) or conjugate kernel scaled by 1/n,
  * for `rows` contiguous rows of n points */
 int tfft_launch_dft(const void *in, void *out, const void *tw, int n, int dir, int64_t rows,

@@ -308,14 +308,14 @@ static int pow2_divisor(int64_t v, int cap)
 
 /* lines per CTA: about 256 threads, at least 8 adjacent lines when the
  * line itself is strided (128-byte segments), at most 8192 points per CTA */
-static int choose_b(int log_l, int64_t n0, int strided)
+static int choose_b(int log_l, int64_t n0, int strided, int ept)
 {
     int64_t L = (int64_t)1 << log_l;
-    int64_t e = L < 16 ? L : 16;
+    int64_t e = L < ept ? L : ept;
     int64_t want = 256 * e / L;
     if (want < 1) want = 1;
     if (strided && want < 8) want = 8;
-    int64_t maxb = 8192 / L;
+    int64_t maxb = (ept == 4 ? 4096 : 8192) / L;
     if (maxb > 32) maxb = 32;
     if (want > maxb) want = maxb;
     if (want < 1) want = 1;
@@ -382,7 +382,14 @@ static int add_pass(struct topeFFT *f, tope_impl *P, int log_l, int64_t ies, int
         }
     }
     int strided = (ies != 1) || (oes != 1);
-    int b = (nl > 0) ? choose_b(log_l, p->n[0], strided) : 1;
+    /* small transforms in FP64 storage (at most 2^16 points in the pass) run
+     * 4 points per thread: more threads, shorter dependent chains each */
+    const int64_t lines_total = p->n[0] * p->n[1] * p->n[2];
+    p->ept = ((P->arith == TFFT_ARITH_F64 || P->arith == TFFT_ARITH_DF64) && log_l >= 2 &&
+              log_l <= 7 && (lines_total << log_l) <= 65536)
+                 ? 4
+                 : 0;
+    int b = (nl > 0) ? choose_b(log_l, p->n[0], strided, p->ept ? 4 : 16) : 1;
     /* few lines (small single transforms): spread them over at least 32 CTAs
      * rather than keep wide tiles */
     while (b > 1 && p->n[0] * p->n[1] * p->n[2] / b < 32) b >>= 1;
@@ -408,7 +415,8 @@ static int add_pass(struct topeFFT *f, tope_impl *P, int log_l, int64_t ies, int
         p->tw_hi = hi;
         p->tw_lo = lo;
     }
-    if (!tfft_pass_supported(log_l, b, P->arith)) return set_status(f, TOPE_ERR_UNSUPPORTED);
+    if (!tfft_pass_supported(log_l, b, P->arith, p->ept))
+        return set_status(f, TOPE_ERR_UNSUPPORTED);
     int st = impl_wl_table(f, P, log_l, &p->tw);
     if (st) return st;
     P->oop[P->npass] = oop;
