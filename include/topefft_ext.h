@@ -115,7 +115,7 @@ void tope3DUploadSpectrum(struct topeFFT *f, struct topePlan3D *t, const double 
  *     same sizes (an FP32 FFT's own rounding error, ~u*sqrt(log2 N));
  *   TOPE_SPLIT_TENSOR: the radix-16 stages as tensor-core GEMMs on 3-way
  *     BF16 splits with FP32 accumulation (lines up to 2^13 per pass, longer
- *     ones in two passes); FP32-level error like TOPE_SPLIT_FAST.  Single
+ *     ones in two or more passes); FP32-level error like TOPE_SPLIT_FAST.  Single
  *     plans only: topeBatchPlanInitF32 rejects it with TOPE_ERR_UNSUPPORTED.
  *     A wait for the tensor cores that gives up is reported by the
  *     synchronous Exec as TOPE_ERR_TIMEOUT.

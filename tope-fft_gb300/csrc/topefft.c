@@ -424,6 +424,52 @@ static int add_pass(struct topeFFT *f, tope_impl *P, int log_l, int64_t ies, int
     return TOPE_SUCCESS;
 }
 
+/*
+ * Out-of-place transform of length 2^lg in `parts` passes: element strides
+ * ies (input) and oes (output), over the lines lines[0..nl) with their own
+ * input and output strides.  With n = n1*n2 (n2 = 2^ceil(lg/parts)):
+ *   pass A transforms along i2 (stride ies*n1) in place, lines i1 (stride ies)
+ *          x lines, and multiplies element k2 by W_n^{i1 k2};
+ *   then, for each k2 (input stride ies*n1, output stride oes), the length-n1
+ *          transform along i1 (stride ies) whose element k1 goes to
+ *          oes*(k1*n2 + k2): one pass into the other buffer, or again this
+ *          split when n1 needs more than one pass.
+ */
+static int plan_split(struct topeFFT *f, tope_impl *P, int lg, int parts, int64_t ies,
+                      int64_t oes, const dimref *lines, int nl)
+{
+    dimref d[5];
+    int st, m;
+    if (nl > 3) return set_status(f, TOPE_ERR_UNSUPPORTED);
+    if (parts == 1) {
+        memcpy(d, lines, sizeof(dimref) * nl);
+        sort_dims(d, nl);
+        m = merge_dims(d, nl);
+        return add_pass(f, P, lg, ies, oes, d, m, 1, 0, 0);
+    }
+    const int l2 = (lg + parts - 1) / parts, l1 = lg - l2;
+    const int64_t n1 = (int64_t)1 << l1, n2 = (int64_t)1 << l2;
+    /* pass A, in place: every line keeps its input strides */
+    for (int i = 0; i < nl; i++) {
+        d[i] = lines[i];
+        d[i].out_stride = d[i].in_stride;
+    }
+    d[nl].count = n1;
+    d[nl].in_stride = d[nl].out_stride = ies;
+    d[nl].is_twiddle = 1;
+    sort_dims(d, nl + 1);
+    m = merge_dims(d, nl + 1);
+    st = add_pass(f, P, l2, ies * n1, ies * n1, d, m, 0, 1, (int64_t)1 << lg);
+    if (st) return st;
+    /* the length-n1 transforms of the columns k2 */
+    memcpy(d, lines, sizeof(dimref) * nl);
+    d[nl].count = n2;
+    d[nl].in_stride = ies * n1;
+    d[nl].out_stride = oes;
+    d[nl].is_twiddle = 0;
+    return plan_split(f, P, l1, parts - 1, ies, oes * n2, d, nl + 1);
+}
+
 /* passes for one axis (0 = x, 1 = y, 2 = z) */
 static int plan_axis(struct topeFFT *f, tope_impl *P, int axis)
 {
@@ -453,33 +499,13 @@ static int plan_axis(struct topeFFT *f, tope_impl *P, int axis)
         sort_dims(d, no);
         int m = merge_dims(d, no);
         st = add_pass(f, P, lg, s, s, d, m, 0, 0, 0);
-        if (st) return st;
     } else {
-        if (lg > 2 * max_lg) return set_status(f, TOPE_ERR_INVALID_SIZE);
-        int l1 = lg / 2, l2 = lg - l1;
-        int64_t n1 = (int64_t)1 << l1, n2 = (int64_t)1 << l2;
-        /* pass A: along i2 (stride s*n1), lines i1 (stride s) x others */
-        dimref d[5];
-        memcpy(d, others, sizeof(dimref) * no);
-        d[no].count = n1;
-        d[no].in_stride = d[no].out_stride = s;
-        d[no].is_twiddle = 1;
-        sort_dims(d, no + 1);
-        int m = merge_dims(d, no + 1);
-        st = add_pass(f, P, l2, s * n1, s * n1, d, m, 0, 1, n);
-        if (st) return st;
-        /* pass B: along i1 (stride s), lines k2 (in s*n1, out s) x others;
-         * element k1 goes to s*(k1*n2 + k2) in the other buffer */
-        memcpy(d, others, sizeof(dimref) * no);
-        d[no].count = n2;
-        d[no].in_stride = s * n1;
-        d[no].out_stride = s;
-        d[no].is_twiddle = 0;
-        sort_dims(d, no + 1);
-        m = merge_dims(d, no + 1);
-        st = add_pass(f, P, l1, s, s * n2, d, m, 1, 0, 0);
-        if (st) return st;
+        /* four-step: two passes up to 2^(2*max_lg) points, one more per
+         * further factor of 2^max_lg */
+        const int parts = lg <= 2 * max_lg ? 2 : (lg + max_lg - 1) / max_lg;
+        st = plan_split(f, P, lg, parts, s, s, others, no);
     }
+    if (st) return st;
     P->axis_count[axis] = P->npass - P->axis_first[axis];
     return TOPE_SUCCESS;
 }
