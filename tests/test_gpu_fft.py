@@ -417,3 +417,47 @@ def test_reference_style_c_driver(T, tmp_path, args):
                     "-lm"], check=True)
     r = subprocess.run([str(exe), *args], capture_output=True, text=True, timeout=120)
     assert r.returncode == 0, r.stdout + r.stderr
+
+
+# plans whose Exec reads back 32 MB or more run their last pass in slices and
+# copy each slice to the host while the next one computes: contiguous slices
+# (batched rows), 2D slices along the sliced line dimension (four-step 1D,
+# the y pass of 2D, the z pass of 3D, three-pass 1D lines)
+READBACK = [((1 << 24, 1, 1), 1), ((1 << 16, 1, 1), 256), ((1 << 12, 1, 1), 2048),
+            ((4096, 4096, 1), 1), ((256, 256, 256), 1), ((64, 128, 512), 1),
+            ((1 << 21, 1, 1), 3)]
+
+
+@pytest.mark.parametrize("shape,batch", READBACK)
+def test_overlapped_readback_matches_download(T, fw, orc, shape, batch):
+    """Exec into a host buffer (sliced last pass, overlapped copies) returns
+    bit for bit what ExecDevice + Download returns, and matches the oracle."""
+    nx, ny, nz = shape
+    x = orc.uniform(nx * ny * nz * batch, SEED0 + 41)
+    if ny == 1 and nz == 1:
+        t = T.TopePlan1D()
+        T.tope1DBatchPlanInit(fw, t, nx, batch, T.C2C, x.copy())
+        ex, ds = T.tope1DExec, T.tope1DDestroy
+    elif nz == 1:
+        t = T.TopePlan2D()
+        T.tope2DPlanInit(fw, t, nx, ny, T.C2C, x.copy())
+        ex, ds = T.tope2DExec, T.tope2DDestroy
+    else:
+        t = T.TopePlan3D()
+        T.tope3DPlanInit(fw, t, nx, ny, nz, T.C2C, x.copy())
+        ex, ds = T.tope3DExec, T.tope3DDestroy
+    T.check(fw)
+    for dir_ in (T.FORWARD, T.INVERSE):
+        T.upload(fw, t, x)
+        got = np.full_like(x, np.nan)
+        ex(fw, t, got, dir_)
+        T.check(fw)
+        T.upload(fw, t, x)
+        T.execDevice(fw, t, dir_)
+        want = np.full_like(x, np.nan)
+        T.download(fw, t, want)
+        T.check(fw)
+        assert np.array_equal(got, want)
+    if batch == 1:
+        assert orc.rel_l2(want, orc.exec(x, nx, ny, nz, dir_=0)) <= tol_fp64(nx * ny * nz)
+    ds(fw, t)

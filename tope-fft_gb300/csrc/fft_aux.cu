@@ -33,6 +33,12 @@ int tfft_d2h(void *dst, const void *src, size_t bytes, void *s)
 {
     return (int)cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, (cudaStream_t)s);
 }
+int tfft_d2h_2d(void *dst, size_t dpitch, const void *src, size_t spitch, size_t width,
+                size_t height, void *s)
+{
+    return (int)cudaMemcpy2DAsync(dst, dpitch, src, spitch, width, height, cudaMemcpyDeviceToHost,
+                                  (cudaStream_t)s);
+}
 int tfft_d2d(void *dst, const void *src, size_t bytes, void *s)
 {
     return (int)cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, (cudaStream_t)s);
@@ -46,6 +52,10 @@ int tfft_stream_create(void **s)
 }
 int tfft_stream_destroy(void *s) { return s ? (int)cudaStreamDestroy((cudaStream_t)s) : 0; }
 int tfft_stream_sync(void *s) { return (int)cudaStreamSynchronize((cudaStream_t)s); }
+int tfft_stream_wait(void *s, void *e)
+{
+    return (int)cudaStreamWaitEvent((cudaStream_t)s, (cudaEvent_t)e, 0);
+}
 int tfft_event_create(void **e)
 {
     cudaEvent_t ev;

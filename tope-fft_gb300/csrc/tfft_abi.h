@@ -130,10 +130,15 @@ int tfft_host_free(void *p);
 int tfft_memset_async(void *p, int v, size_t bytes, void *stream);
 int tfft_h2d(void *dst, const void *src, size_t bytes, void *stream);
 int tfft_d2h(void *dst, const void *src, size_t bytes, void *stream);
+/* height rows of width bytes, rows pitch bytes apart on each side */
+int tfft_d2h_2d(void *dst, size_t dpitch, const void *src, size_t spitch, size_t width,
+                size_t height, void *stream);
 int tfft_d2d(void *dst, const void *src, size_t bytes, void *stream);
 int tfft_stream_create(void **s);
 int tfft_stream_destroy(void *s);
 int tfft_stream_sync(void *s);
+/* later work on stream s waits for event e */
+int tfft_stream_wait(void *s, void *e);
 int tfft_event_create(void **e);
 int tfft_event_destroy(void *e);
 int tfft_event_record(void *e, void *stream);

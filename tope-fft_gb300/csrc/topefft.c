@@ -80,10 +80,17 @@ typedef struct tope_evpair {
     void *a, *b;
 } tope_evpair;
 
+/* slices of the last pass whose read-back overlaps the next slice */
+#define RB_SLICES 8
+
 typedef struct tope_fw {
     unsigned magic;
     void *stream;
     tope_evpair pair;
+    /* overlapped read-back: a copy stream and one event per slice, made on
+     * first use */
+    void *copy;
+    void *slice_ev[RB_SLICES];
 } tope_fw;
 
 uint64_t profileThis(void *event)
@@ -134,8 +141,11 @@ static void fw_close(struct topeFFT *f)
     tope_fw *w = fw_of(f);
     if (!w) return;
     tfft_stream_sync(w->stream);
+    if (w->copy) tfft_stream_sync(w->copy);
     tfft_event_destroy(w->pair.a);
     tfft_event_destroy(w->pair.b);
+    for (int i = 0; i < RB_SLICES; i++) tfft_event_destroy(w->slice_ev[i]);
+    tfft_stream_destroy(w->copy);
     tfft_stream_destroy(w->stream);
     w->magic = 0;
     free(w);
@@ -778,19 +788,27 @@ static void settle(tope_impl *P, uint64_t *t_kernel)
     }
 }
 
-/* Queue passes [first, first+count) on the current buffer.  conj/scale make
- * the sequence an inverse when dir == INVERSE. */
-static int run_passes(struct topeFFT *f, tope_impl *P, int first, int count, int dir,
-                      double scale)
+/* launch arguments of pass i inside the sequence [first, last] on the
+ * current buffer: conj/scale make the sequence an inverse when dir == INVERSE */
+static tfft_pass pass_args(const tope_impl *P, int i, int first, int last, int dir, double scale)
+{
+    tfft_pass p = P->pass[i];
+    p.in = P->buf[P->cur];
+    p.out = P->oop[i] ? P->buf[1 - P->cur] : P->buf[P->cur];
+    p.conj_in = (dir == INVERSE) && (i == first);
+    p.conj_out = (dir == INVERSE) && (i == last);
+    p.scale = i == last ? scale : 1.0;
+    return p;
+}
+
+/* Queue passes [first, first+count) on the current buffer, but the last
+ * `hold` of them, which the caller launches itself. */
+static int run_passes_hold(struct topeFFT *f, tope_impl *P, int first, int count, int dir,
+                           double scale, int hold)
 {
     void *stream = f->command_queue;
-    for (int i = first; i < first + count; i++) {
-        tfft_pass p = P->pass[i];
-        p.in = P->buf[P->cur];
-        p.out = P->oop[i] ? P->buf[1 - P->cur] : P->buf[P->cur];
-        p.conj_in = (dir == INVERSE) && (i == first);
-        p.conj_out = (dir == INVERSE) && (i == first + count - 1);
-        p.scale = (i == first + count - 1) ? scale : 1.0;
+    for (int i = first; i < first + count - hold; i++) {
+        tfft_pass p = pass_args(P, i, first, first + count - 1, dir, scale);
         void **ev = f->pass_timing ? pev_take(P, i) : NULL;
         if (ev) tfft_event_record(ev[0], stream);
         int rc = tfft_launch_pass(&p, stream);
@@ -801,6 +819,12 @@ static int run_passes(struct topeFFT *f, tope_impl *P, int first, int count, int
     return TOPE_SUCCESS;
 }
 
+static int run_passes(struct topeFFT *f, tope_impl *P, int first, int count, int dir,
+                      double scale)
+{
+    return run_passes_hold(f, P, first, count, dir, scale, 0);
+}
+
 /* where a real-data plan's spectrum lives: its own buffer (1D) or the
  * current buffer of its spectrum plan (2D/3D) */
 static void *spec_buf(const tope_impl *P)
@@ -808,8 +832,9 @@ static void *spec_buf(const tope_impl *P)
     return P->specp ? P->specp->buf[P->specp->cur] : P->spec;
 }
 
-/* queue the whole transform; events bracket the kernels */
-static int impl_exec_async(struct topeFFT *f, tope_impl *P, int dir)
+/* queue the whole transform; events bracket the kernels.  hold = 1 (FFT
+ * plans only) leaves the last pass and the closing events to the caller. */
+static int impl_exec_async(struct topeFFT *f, tope_impl *P, int dir, int hold)
 {
     void *stream = f->command_queue;
     int rc, st = TOPE_SUCCESS;
@@ -838,7 +863,7 @@ static int impl_exec_async(struct topeFFT *f, tope_impl *P, int dir)
         if (P->npass == 0) {
             /* all axes of length 1: identity (inverse divides by 1) */
         } else {
-            st = run_passes(f, P, 0, P->npass, dir, scale);
+            st = run_passes_hold(f, P, 0, P->npass, dir, scale, hold);
         }
     } else if (P->mode == MODE_N2) {
         if ((rc = tfft_launch_n2(P->buf[P->cur], dir, stream))) st = cuda_status(f, rc);
@@ -871,8 +896,10 @@ static int impl_exec_async(struct topeFFT *f, tope_impl *P, int dir)
         if (!st && P->specp) st = run_passes(f, P->specp, 0, P->specp->npass, FORWARD, 1.0);
         P->spec_cur = 1;
     }
-    tfft_event_record(P->kev.b, stream);
-    tfft_event_record(w->pair.b, stream);
+    if (!hold) {
+        tfft_event_record(P->kev.b, stream);
+        tfft_event_record(w->pair.b, stream);
+    }
     P->pending = 1;
     return st;
 }
@@ -888,6 +915,141 @@ static void *cur_data(const tope_impl *P, size_t *bytes)
     return P->buf[P->cur];
 }
 
+/* the status of a finished exec: a wait for the tensor cores that gave up
+ * leaves a flag on the device */
+static int tc_status(struct topeFFT *f, const tope_impl *P, void *stream)
+{
+    if (P->arith == TFFT_ARITH_TC) {
+        int flag = 0, rc;
+        if ((rc = tfft_tc_error(&flag, stream))) return cuda_status(f, rc);
+        if (flag) return set_status(f, TOPE_ERR_TIMEOUT);
+    }
+    return set_status(f, TOPE_SUCCESS);
+}
+
+/*
+ * Read-back overlapped with the last pass.  That pass runs as up to RB_SLICES
+ * launches, each over a slice of its outermost line dimension, and each
+ * slice's output goes to the host on the framework's copy stream while the
+ * next slice computes.  A slice's output must be a dense rectangle: a
+ * contiguous range when the element axis lies inside the sliced dimension,
+ * else `rows` rows (one per element of the line) of `width` elements, `pitch`
+ * apart.  Returns 0 when the plan does not qualify (the read-back then
+ * follows the transform).
+ */
+#define RB_MIN_BYTES ((size_t)32 << 20) /* below this a single copy is as fast */
+#define RB_MIN_ROW 2048                 /* bytes per row of a 2D slice copy */
+
+typedef struct rb_geom {
+    int dim;       /* sliced line dimension of the last pass */
+    int64_t step;  /* lines of that dimension per slice */
+    int64_t rows;  /* 0: contiguous slices; else rows per slice */
+    int64_t pitch; /* elements between rows */
+} rb_geom;
+
+static int rb_plan(const struct topeFFT *f, const tope_impl *P, rb_geom *g)
+{
+    if (P->mode != MODE_FFT || P->real || P->npass < 1 || f->pass_timing) return 0;
+    if ((size_t)P->total * (size_t)P->es < RB_MIN_BYTES) return 0;
+    const tfft_pass *p = &P->pass[P->npass - 1];
+    /* a slice must not shift a line index the pass itself uses */
+    if (p->post_tw || p->tab0 || p->tab1) return 0;
+    int64_t cnt[4], str[4];
+    int nd = 0, dim = -1;
+    for (int i = 0; i < 3; i++) {
+        if (p->n[i] <= 1) continue;
+        if (dim < 0 || p->os[i] > p->os[dim]) dim = i;
+        cnt[nd] = p->n[i];
+        str[nd++] = p->os[i];
+    }
+    if (dim < 0) return 0;
+    cnt[nd] = (int64_t)1 << p->log_l;
+    str[nd++] = p->oes;
+    /* dense output: by increasing stride, each stride is the product of the
+     * counts below it */
+    for (int i = 1; i < nd; i++)
+        for (int j = i; j > 0 && str[j] < str[j - 1]; j--) {
+            int64_t t = str[j];
+            str[j] = str[j - 1];
+            str[j - 1] = t;
+            t = cnt[j];
+            cnt[j] = cnt[j - 1];
+            cnt[j - 1] = t;
+        }
+    int64_t expect = 1;
+    for (int i = 0; i < nd; i++) {
+        if (str[i] != expect) return 0;
+        expect *= cnt[i];
+    }
+    if (expect != P->total) return 0;
+    const int64_t n = p->n[dim];
+    int64_t step = (n + RB_SLICES - 1) / RB_SLICES;
+    if (dim == 0) step = (step + p->b_tile - 1) / p->b_tile * p->b_tile;
+    if (step >= n) return 0;
+    g->dim = dim;
+    g->step = step;
+    g->rows = 0;
+    g->pitch = 0;
+    if (p->oes > p->os[dim]) {
+        g->rows = (int64_t)1 << p->log_l;
+        g->pitch = p->oes;
+        if ((size_t)step * (size_t)p->os[dim] * (size_t)P->es < RB_MIN_ROW) return 0;
+        if ((size_t)p->oes * (size_t)P->es >= ((size_t)1 << 31)) return 0;
+    }
+    return 1;
+}
+
+/* the framework's copy stream and slice events (made once) */
+static int rb_open(tope_fw *w)
+{
+    if (w->copy) return 0;
+    for (int i = 0; i < RB_SLICES; i++)
+        if (!w->slice_ev[i] && tfft_event_create(&w->slice_ev[i])) return 1;
+    return tfft_stream_create(&w->copy) ? 1 : 0;
+}
+
+/* launch the last pass slice by slice and copy each slice's output to d on
+ * the copy stream; the caller synchronises both streams */
+static int rb_run(struct topeFFT *f, tope_impl *P, const rb_geom *g, int dir, double scale,
+                  char *d)
+{
+    tope_fw *w = fw_of(f);
+    void *stream = f->command_queue;
+    const int last = P->npass - 1;
+    tfft_pass p = pass_args(P, last, 0, last, dir, scale);
+    const int64_t n = p.n[g->dim];
+    const size_t es = (size_t)P->es;
+    char *src = (char *)p.out;
+    int ns = 0, rc;
+    for (int64_t a = 0; a < n; a += g->step, ns++) {
+        tfft_pass q = p;
+        q.n[g->dim] = (a + g->step <= n) ? g->step : n - a;
+        q.in = (const char *)p.in + (size_t)(a * p.is[g->dim]) * es;
+        q.out = (char *)p.out + (size_t)(a * p.os[g->dim]) * es;
+        if ((rc = tfft_launch_pass(&q, stream))) return cuda_status(f, rc);
+        if ((rc = tfft_event_record(w->slice_ev[ns], stream))) return cuda_status(f, rc);
+    }
+    if (P->oop[last]) P->cur = 1 - P->cur;
+    tfft_event_record(P->kev.b, stream);
+    tfft_event_record(w->pair.b, stream);
+    ns = 0;
+    for (int64_t a = 0; a < n; a += g->step, ns++) {
+        const int64_t lines = (a + g->step <= n) ? g->step : n - a;
+        const size_t off = (size_t)(a * p.os[g->dim]) * es;
+        const size_t width = (size_t)(lines * p.os[g->dim]) * es;
+        if ((rc = tfft_stream_wait(w->copy, w->slice_ev[ns]))) return cuda_status(f, rc);
+        if (ns == 0) tfft_event_record(P->mev.a, w->copy);
+        if (g->rows)
+            rc = tfft_d2h_2d(d + off, (size_t)g->pitch * es, src + off, (size_t)g->pitch * es,
+                             width, (size_t)g->rows, w->copy);
+        else
+            rc = tfft_d2h(d + off, src + off, width, w->copy);
+        if (rc) return cuda_status(f, rc);
+    }
+    tfft_event_record(P->mev.b, w->copy);
+    return TOPE_SUCCESS;
+}
+
 /* synchronous: exec, then read back into d (if non-NULL).  es_caller is the
  * element size the calling entry point deals in (16 FP64, 8 FP32). */
 static int impl_exec(struct topeFFT *f, tope_impl *P, void *d, int es_caller, int dir,
@@ -901,7 +1063,27 @@ static int impl_exec(struct topeFFT *f, tope_impl *P, void *d, int es_caller, in
         if (!d) return set_status(f, TOPE_ERR_INVALID_ARG);
         if ((rc = tfft_h2d(P->buf[P->cur], d, 32, stream))) return cuda_status(f, rc);
     }
-    st = impl_exec_async(f, P, dir);
+    rb_geom g;
+    if (d && rb_plan(f, P, &g) && !rb_open(fw_of(f))) {
+        /* the last pass in slices, each read back while the next computes */
+        tope_fw *w = fw_of(f);
+        st = impl_exec_async(f, P, dir, 1);
+        if (!st) st = rb_run(f, P, &g, dir, dir == INVERSE ? 1.0 / (double)P->volume : 1.0,
+                             (char *)d);
+        rc = tfft_stream_sync(stream);
+        int rc2 = tfft_stream_sync(w->copy);
+        if (st) {
+            P->pending = 0;
+            return st;
+        }
+        if (rc || rc2) return cuda_status(f, rc ? rc : rc2);
+        settle(P, t_kernel);
+        uint64_t ns = 0;
+        tfft_event_elapsed_ns(P->mev.a, P->mev.b, &ns);
+        *t_mem += ns;
+        return tc_status(f, P, stream);
+    }
+    st = impl_exec_async(f, P, dir, 0);
     if (st) {
         tfft_stream_sync(stream);
         return st;
@@ -924,13 +1106,7 @@ static int impl_exec(struct topeFFT *f, tope_impl *P, void *d, int es_caller, in
         tfft_event_elapsed_ns(P->mev.a, P->mev.b, &ns);
         *t_mem += ns;
     }
-    if (P->arith == TFFT_ARITH_TC) {
-        /* a wait for the tensor cores that gave up leaves a flag */
-        int flag = 0;
-        if ((rc = tfft_tc_error(&flag, stream))) return cuda_status(f, rc);
-        if (flag) return set_status(f, TOPE_ERR_TIMEOUT);
-    }
-    return set_status(f, TOPE_SUCCESS);
+    return tc_status(f, P, stream);
 }
 
 static int impl_axis(struct topeFFT *f, tope_impl *P, int axis, uint64_t *t_kernel)
@@ -1080,7 +1256,7 @@ void tope1DExecDevice(struct topeFFT *f, struct topePlan1D *t, int dir)
 {
     tope_impl *P = t ? impl_of(f, t->impl) : NULL;
     if (!P) return;
-    if (impl_exec_async(f, P, dir) == TOPE_SUCCESS) set_status(f, TOPE_SUCCESS);
+    if (impl_exec_async(f, P, dir, 0) == TOPE_SUCCESS) set_status(f, TOPE_SUCCESS);
     sync_fields_1d(t, P);
 }
 
@@ -1252,7 +1428,7 @@ void tope2DExecDevice(struct topeFFT *f, struct topePlan2D *t, int dir)
 {
     tope_impl *P = t ? impl_of(f, t->impl) : NULL;
     if (!P) return;
-    if (impl_exec_async(f, P, dir) == TOPE_SUCCESS) set_status(f, TOPE_SUCCESS);
+    if (impl_exec_async(f, P, dir, 0) == TOPE_SUCCESS) set_status(f, TOPE_SUCCESS);
     t->data = P->buf[P->cur];
 }
 
@@ -1393,7 +1569,7 @@ void tope3DExecDevice(struct topeFFT *f, struct topePlan3D *t, int dir)
 {
     tope_impl *P = t ? impl_of(f, t->impl) : NULL;
     if (!P) return;
-    if (impl_exec_async(f, P, dir) == TOPE_SUCCESS) set_status(f, TOPE_SUCCESS);
+    if (impl_exec_async(f, P, dir, 0) == TOPE_SUCCESS) set_status(f, TOPE_SUCCESS);
     t->data = P->buf[P->cur];
 }
 
