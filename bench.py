@@ -70,8 +70,11 @@ WORKLOADS = {
                     "desc": "1D real-to-complex FP64, N=2^24 uniform[-1,1) reals, forward (R2C) "
                             "+ inverse (C2R); GFLOP/s counts 2.5 N log2 N per direction"},
     "1d_1e6": {"dims": (1000000, 1, 1), "batch": 1,
-               "desc": "1D C2C FP64, N=10^6 (not a power of two: Bluestein over 2^21-point "
-                       "sub-transforms), forward+inverse, uniform[-1,1) re/im"},
+               "desc": "1D C2C FP64, N=10^6 = 2^6 5^6 (not a power of two: two mixed-radix "
+                       "passes of 1000-point lines), forward+inverse, uniform[-1,1) re/im"},
+    "1d_prime": {"dims": (999983, 1, 1), "batch": 1,
+                 "desc": "1D C2C FP64, N=999983 (prime: Bluestein over 2^a 3^b 5^c 7^d-point "
+                         "sub-transforms), forward+inverse, uniform[-1,1) re/im"},
     "batch_uneven": {"uneven": True, "f32": False,
                      "desc": "uneven batch: 20,000 1D transforms N=2^k, k~U{6..16}, plus 500 2D "
                              "transforms with sides from {64..1024}, uniform re/im, FP64, "
@@ -167,18 +170,25 @@ def flops_per_step(wl: dict) -> float:
 
 def pass_points(wl: dict) -> int:
     """Complex points one pass launch of the dominant kernel moves: the array,
-    its packed half for real data, or the power-of-two sub-transform of a
-    Bluestein plan."""
+    its packed half for real data, or, for a 1D length with a prime factor
+    above 13, the 2^a 3^b 5^c 7^d sub-transform of its Bluestein plan."""
     nx, ny, nz = wl["dims"]
     n = nx * ny * nz
     if wl.get("real"):
         return n // 2 * wl["batch"]
-    if ny * nz == 1 and n & (n - 1) and n >= 128:
-        m = 1
-        while m < 2 * n - 1:
-            m <<= 1
+    if ny * nz == 1 and n >= 128 and not smooth(n, (2, 3, 5, 7, 11, 13)):
+        m = 2 * n - 1
+        while not smooth(m, (2, 3, 5, 7)):
+            m += 1
         return m * wl["batch"]
     return n * wl["batch"]
+
+
+def smooth(n: int, primes) -> bool:
+    for p in primes:
+        while n % p == 0:
+            n //= p
+    return n == 1
 
 
 def p_min(n: int, fp32: bool = False) -> int:
@@ -491,8 +501,9 @@ def run_gpu(args, wl: dict) -> dict:
         roof = {"bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(ach / peak, 4), "peak_source": peak_kind,
                 "traffic": ncu_traffic(args.workload, SPLIT_ARITH[args.split] if f32 else args.arith),
-                "kernel": f"pass_kernel L=2^{dom['log_l']} B={dom['b_tile']} "
-                          f"({dom['ctas']} CTAs x {dom['threads']} threads)",
+                "kernel": (f"pass_kernel L=2^{dom['log_l']}" if dom["log_l"] >= 0 else
+                           f"mixed_kernel L={dom['len']}") +
+                          f" B={dom['b_tile']} ({dom['ctas']} CTAs x {dom['threads']} threads)",
                 "launch_us": round(avg_ns / 1e3, 2),
                 "bytes_per_launch": bytes_per_launch,
                 "fp64_pipe_tflops_measured": FP64_PIPE_TFLOPS}

@@ -209,8 +209,9 @@ void topeSetPassTiming(struct topeFFT *f, int enable);
  * (run twice per transform), as for topePassInfo. */
 int topePassTimes(struct topeFFT *f, void *impl, uint64_t *ns, uint64_t *launches, int max);
 void topeResetPassTimes(struct topeFFT *f, void *impl);
-/* Geometry of pass i of a plan: {log2 L, lines per CTA, CTAs, threads per
- * CTA, out-of-place, four-step twiddle}; returns 0, or -1 if i is out of range. */
+/* Geometry of pass i of a plan: {log2 L (or -L for a line length L that is
+ * not a power of two), lines per CTA, CTAs, threads per CTA, out-of-place,
+ * four-step twiddle}; returns 0, or -1 if i is out of range. */
 int topePassInfo(struct topeFFT *f, void *impl, int i, int64_t info[6]);
 
 /* ---- allocation-free 1D transform ---------------------------------------- */

@@ -142,6 +142,8 @@ class Oracle:
     # long-double oracles ----------------------------------------------------
     def fft_ld(self, d: np.ndarray, nx: int, ny: int = 1, nz: int = 1, dir_: int = 1) -> np.ndarray:
         out = np.ascontiguousarray(d, dtype=np.float64).copy()
+        if ny == 1 and nz == 1 and nx & (nx - 1):
+            return self.dft_ld(out, nx, dir_)
         if ny == 1 and nz == 1:
             self.lib.oracle_fft_ld(_ptr(out), nx, dir_)
         else:

@@ -368,6 +368,30 @@ static void fft_ld_line(ld *xr, ld *xi, int64_t n, const ld *tr, const ld *ti, i
     }
 }
 
+/* unscaled O(n^2) sum for an axis whose length is not a power of two (the
+ * same sum as oracle_dft_ld below, on one line; y is scratch) */
+static void dft_ld_line(ld *xr, ld *xi, int n, const ld *tr, const ld *ti, int dir, ld *yr,
+                        ld *yi)
+{
+    for (int k = 0; k < n; k++) {
+        ld sr = 0, si = 0;
+        for (int j = 0; j < n; j++) {
+            int64_t m = ((int64_t)j * k) % n;
+            ld wr = tr[m], wi = dir ? ti[m] : -ti[m];
+            sr += xr[j] * wr - xi[j] * wi;
+            si += xr[j] * wi + xi[j] * wr;
+        }
+        yr[k] = sr;
+        yi[k] = si;
+    }
+    for (int k = 0; k < n; k++) {
+        xr[k] = yr[k];
+        xi[k] = yi[k];
+    }
+}
+
+/* every line of one axis: the radix-2 long-double FFT for 2^k points, the
+ * O(n^2) sum for other lengths */
 static void fft_ld_axis(double *d, int nx, int ny, int nz, int axis, int dir)
 {
     int n;
@@ -379,6 +403,7 @@ static void fft_ld_axis(double *d, int nx, int ny, int nz, int axis, int dir)
 #pragma omp parallel
     {
         ld *xr = (ld *)malloc(sizeof(ld) * n), *xi = (ld *)malloc(sizeof(ld) * n);
+        ld *yr = (ld *)malloc(sizeof(ld) * n), *yi = (ld *)malloc(sizeof(ld) * n);
 #pragma omp for schedule(static)
         for (int64_t line = 0; line < lines; line++) {
             int64_t base = line_base(nx, ny, axis, line);
@@ -386,7 +411,8 @@ static void fft_ld_axis(double *d, int nx, int ny, int nz, int axis, int dir)
                 xr[i] = d[2 * (base + stride * i)];
                 xi[i] = d[2 * (base + stride * i) + 1];
             }
-            fft_ld_line(xr, xi, n, tr, ti, dir);
+            if (n & (n - 1)) dft_ld_line(xr, xi, n, tr, ti, dir, yr, yi);
+            else fft_ld_line(xr, xi, n, tr, ti, dir);
             ld s = dir ? 1.0L : 1.0L / (ld)n;
             for (int i = 0; i < n; i++) {
                 d[2 * (base + stride * i)] = (double)(xr[i] * s);
@@ -395,6 +421,8 @@ static void fft_ld_axis(double *d, int nx, int ny, int nz, int axis, int dir)
         }
         free(xr);
         free(xi);
+        free(yr);
+        free(yi);
     }
     free(tr);
     free(ti);

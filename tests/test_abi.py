@@ -119,7 +119,7 @@ def test_null_arguments_are_rejected(T):
     # framework never initialised: PlanInit must fail cleanly, not crash
     T.lib.tope2DPlanInit(ctypes.byref(f), None, 4, 4, T.C2C, None)
     assert f.error == T.TOPE_ERR_INVALID_ARG
-    T.tope2DPlanInit(f, t, 6, 4, T.C2C, np.zeros(48))
+    T.tope2DPlanInit(f, t, 34, 4, T.C2C, np.zeros(272))  # 34 = 2 * 17
     assert f.error == T.TOPE_ERR_INVALID_SIZE
     T.tope2DPlanInit(f, t, 4, 4, 5, np.zeros(32))  # neither C2C nor R2C
     assert f.error == T.TOPE_ERR_UNSUPPORTED

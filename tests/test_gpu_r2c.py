@@ -113,7 +113,7 @@ def test_r2c_rejects_bad_shapes_and_split_precision(T, fw):
     t2 = T.TopePlan2D()
     T.tope2DPlanInit(fw, t2, 7, 8, T.R2C, np.zeros(128))  # odd x
     assert fw.error == T.TOPE_ERR_INVALID_SIZE and not t2.impl
-    T.tope2DPlanInit(fw, t2, 8, 6, T.R2C, np.zeros(128))  # y not a power of two
+    T.tope2DPlanInit(fw, t2, 8, 17, T.R2C, np.zeros(8 * 17))  # y with a prime factor > 13
     assert fw.error == T.TOPE_ERR_INVALID_SIZE and not t2.impl
 
 
@@ -146,7 +146,9 @@ def destroy_nd(T, f, t):
 
 
 ND = [(8, 4, 1), (64, 32, 1), (512, 256, 1), (4096, 4096, 1), (2, 2, 1), (16, 8, 4),
-      (64, 32, 16), (256, 256, 256), (32, 1 << 14, 1)]
+      (64, 32, 16), (256, 256, 256), (32, 1 << 14, 1),
+      # sides with factors 3, 5, 7 (x/2 = 50, 45, 21): mixed-radix passes
+      (100, 60, 1), (90, 12, 14), (42, 25, 1)]
 
 
 @pytest.mark.parametrize("dims", ND, ids=lambda d: "x".join(map(str, d)))

@@ -165,3 +165,20 @@ def test_bluestein_ld_matches_direct_sum(orc, n, dir_):
     p = 1 << 11
     y = orc.uniform(p, 301)
     assert orc.rel_l2(orc.bluestein_ld(y, p, dir_), orc.fft_ld(y, p, dir_=dir_)) <= 5e-17
+
+
+@pytest.mark.parametrize("shape", [(6, 10, 1), (12, 8, 5), (7, 3, 9), (16, 15, 1)])
+@pytest.mark.parametrize("dir_", [1, 0], ids=["fwd", "inv"])
+def test_nd_long_double_any_sides(orc, shape, dir_):
+    """The long-double ND oracle on sides that are not powers of two (the
+    O(n^2) sum along such axes) agrees with numpy's FFT, and its 1D form
+    with the direct sum."""
+    nx, ny, nz = shape
+    x = orc.uniform(nx * ny * nz, 400 + nx)
+    got = orc.fft_ld(x, nx, ny, nz, dir_=dir_)
+    c = (x[0::2] + 1j * x[1::2]).reshape(nz, ny, nx)
+    want = np.fft.fftn(c) if dir_ == 1 else np.fft.ifftn(c)
+    w = np.empty(2 * c.size)
+    w[0::2], w[1::2] = want.real.ravel(), want.imag.ravel()
+    assert orc.rel_l2(got, w) <= 1e-15
+    assert orc.rel_l2(orc.fft_ld(x[: 2 * nx], nx, dir_=dir_), orc.dft_ld(x[: 2 * nx], nx, dir_)) <= 1e-17

@@ -70,6 +70,15 @@ struct ArithF64 {
     }
     static __device__ __forceinline__ TW tw_mul(TW a, TW b) { return mul_tw(a, b); }
 
+    /* real constants (odd-radix butterflies): a * c and acc + a * c */
+    using R = double;
+    static __host__ __device__ constexpr R rc(double d, float, float) { return d; }
+    static __device__ __forceinline__ C mulr(C a, R c) { return make_double2(a.x * c, a.y * c); }
+    static __device__ __forceinline__ C fmar(C acc, C a, R c)
+    {
+        return make_double2(fma(a.x, c, acc.x), fma(a.y, c, acc.y));
+    }
+
     /* storage conversion; FP64 needs no tile scaling */
     static constexpr bool kScaled = false;
     static __device__ __forceinline__ C load_s(double2 v, int) { return v; }
@@ -322,6 +331,18 @@ __host__ __device__ __forceinline__ df2 ddiffprod(df2 a, df2 b, df2 c, df2 d)
 #define TFFT_DF_S8 {0x1.87de2ap-2f, 0x1.abaa58p-28f}
 #define TFFT_DF_R2 {0x1.6a09e6p-1f, 0x1.9fcef4p-27f}
 
+/* a scale factor as a (hi, lo) float pair */
+__host__ __device__ __forceinline__ df2 scale_pair(double s)
+{
+    const float h = (float)s;
+    return df2{h, (float)(s - (double)h)};
+}
+/* is s a power of two (the 1/N of a power-of-two transform)? */
+__host__ __device__ __forceinline__ bool pow2_scale(double s)
+{
+    return (d2ull(s) & 0xfffffffffffffull) == 0;
+}
+
 struct ArithDF64 {
     struct C {
         df2 r, i;
@@ -342,9 +363,15 @@ struct ArithDF64 {
     static __host__ __device__ __forceinline__ double2 store_s(C v, int delta, double scale)
     {
         int ds = 0;
-        if (scale != 1.0) { /* scale is 2^-k: fold it into the exponent */
+        if (scale != 1.0) {
             unsigned long long sb = d2ull(scale);
-            ds = (int)((sb >> 52) & 0x7ff) - 1023;
+            if (sb & 0xfffffffffffffull) {
+                /* 1/N for N not a power of two: a pair product */
+                v.r = dmul(v.r, scale_pair(scale));
+                v.i = dmul(v.i, scale_pair(scale));
+            } else { /* 2^-k: fold it into the exponent */
+                ds = (int)((sb >> 52) & 0x7ff) - 1023;
+            }
         }
         return make_double2(join_double(v.r.h, v.r.l, delta + ds),
                             join_double(v.i.h, v.i.l, delta + ds));
@@ -428,6 +455,17 @@ struct ArithDF64 {
     {
         return __ldg(reinterpret_cast<const float4 *>(tab) + m);
     }
+    /* real constants as (hi, lo) pairs: a * c and acc + a * c */
+    using R = df2;
+    static __host__ __device__ constexpr R rc(double, float h, float l) { return df2{h, l}; }
+    static __host__ __device__ __forceinline__ C mulr(C a, R c)
+    {
+        C o;
+        o.r = dmul(a.r, c);
+        o.i = dmul(a.i, c);
+        return o;
+    }
+    static __host__ __device__ __forceinline__ C fmar(C acc, C a, R c) { return add(acc, mulr(a, c)); }
     static __host__ __device__ __forceinline__ TW tw_mul(TW a, TW b)
     {
         C x;
@@ -460,6 +498,11 @@ struct ArithDF32 : ArithDF64 {
     }
     static __host__ __device__ __forceinline__ float2 store_s(C v, int, double scale)
     {
+        if (scale != 1.0 && !pow2_scale(scale)) {
+            v.r = dmul(v.r, scale_pair(scale));
+            v.i = dmul(v.i, scale_pair(scale));
+            return make_float2(add_rn(v.r.h, v.r.l), add_rn(v.i.h, v.i.l));
+        }
         float2 o = make_float2(add_rn(v.r.h, v.r.l), add_rn(v.i.h, v.i.l));
         if (scale != 1.0) {
             const float s = (float)scale; /* a power of two: exact */
@@ -487,6 +530,8 @@ struct ArithF32 {
     static __host__ __device__ __forceinline__ float2 store_s(C v, int, double scale)
     {
         if (scale != 1.0) {
+            if (!pow2_scale(scale)) return make_float2(mulc(v.x, scale_pair(scale)),
+                                                       mulc(v.y, scale_pair(scale)));
             const float s = (float)scale; /* a power of two: exact */
             v.x *= s;
             v.y *= s;
@@ -546,6 +591,18 @@ struct ArithF32 {
     static __host__ __device__ __forceinline__ TW tw_mul(TW a, TW b)
     {
         return ArithDF64::tw_mul(a, b);
+    }
+    /* real constants as (hi, lo) pairs: a * c and acc + a * c */
+    using R = df2;
+    static __host__ __device__ constexpr R rc(double, float h, float l) { return df2{h, l}; }
+    static __host__ __device__ __forceinline__ C mulr(C a, R c)
+    {
+        return make_float2(mulc(a.x, c), mulc(a.y, c));
+    }
+    static __host__ __device__ __forceinline__ C fmar(C acc, C a, R c)
+    {
+        return make_float2(fmaf_(a.x, c.h, fmaf_(a.x, c.l, acc.x)),
+                           fmaf_(a.y, c.h, fmaf_(a.y, c.l, acc.y)));
     }
 };
 

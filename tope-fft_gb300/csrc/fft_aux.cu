@@ -91,6 +91,26 @@ __device__ __forceinline__ double2 w_pow2(int64_t m, int log_n)
     return make_double2(c, -s);
 }
 
+/* exp(-2 pi i m / n) for any n, m < n: the angle pi*2m/n is first brought
+ * to pi*x with |x| <= 1/2 by exact integer steps (W^m = conj(W^(n-m)) and a
+ * half turn), so the one rounding of the quotient x stays below 2^-54. */
+__device__ __forceinline__ double2 w_any(int64_t m, int64_t n)
+{
+    int64_t num = 2 * m; /* angle pi * num / n, num in [0, 2n) */
+    if (num > n) num -= 2 * n; /* (-n, n] */
+    bool flip = false;
+    if (2 * num > n) {
+        num -= n;
+        flip = true;
+    } else if (2 * num < -n) {
+        num += n;
+        flip = true;
+    }
+    double s, c;
+    sincospi((double)num / (double)n, &s, &c);
+    return flip ? make_double2(-c, s) : make_double2(c, -s);
+}
+
 __device__ __forceinline__ void put_tw(void *tab, int64_t i, double2 w, int arith)
 {
     if (arith == TFFT_ARITH_F64) {
@@ -110,14 +130,22 @@ __global__ void k_twiddle(void *tw, int log_l, int arith)
         put_tw(tw, m, w_pow2(m, log_l), arith);
 }
 
-__global__ void k_fourstep(void *hi, void *lo, int log_n, int shift, int arith)
+/* log_n < 0: n is not a power of two */
+__global__ void k_fourstep(void *hi, void *lo, int64_t n, int log_n, int shift, int arith)
 {
-    const int64_t nlo = int64_t(1) << shift, nhi = int64_t(1) << (log_n - shift);
+    const int64_t nlo = int64_t(1) << shift, nhi = (n + nlo - 1) >> shift;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nlo + nhi;
          i += (int64_t)gridDim.x * blockDim.x) {
-        if (i < nlo) put_tw(lo, i, w_pow2(i, log_n), arith);
-        else put_tw(hi, i - nlo, w_pow2((i - nlo) << shift, log_n), arith);
+        const int64_t m = i < nlo ? i : (i - nlo) << shift;
+        const double2 w = log_n >= 0 ? w_pow2(m, log_n) : w_any(m % n, n);
+        put_tw(i < nlo ? lo : hi, i < nlo ? i : i - nlo, w, arith);
     }
+}
+
+__global__ void k_table_any(void *tw, int len, int arith)
+{
+    for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < len; m += gridDim.x * blockDim.x)
+        put_tw(tw, m, w_any(m, len), arith);
 }
 
 __global__ void k_bitrev(int *rev, int log2n)
@@ -362,8 +390,15 @@ int tfft_fourstep_tables(void *hi, void *lo, int64_t n, int shift, int arith, vo
 {
     int log_n = 0;
     while ((int64_t(1) << log_n) < n) log_n++;
-    const int64_t cnt = (int64_t(1) << shift) + (n >> shift);
-    k_fourstep<<<grid_for(cnt, 256), 256, 0, (cudaStream_t)s>>>(hi, lo, log_n, shift, arith);
+    if ((int64_t(1) << log_n) != n) log_n = -1;
+    const int64_t nlo = int64_t(1) << shift, cnt = nlo + ((n + nlo - 1) >> shift);
+    k_fourstep<<<grid_for(cnt, 256), 256, 0, (cudaStream_t)s>>>(hi, lo, n, log_n, shift, arith);
+    return (int)cudaGetLastError();
+}
+
+int tfft_table_any(void *tw, int len, int arith, void *s)
+{
+    k_table_any<<<grid_for(len, 256), 256, 0, (cudaStream_t)s>>>(tw, len, arith);
     return (int)cudaGetLastError();
 }
 

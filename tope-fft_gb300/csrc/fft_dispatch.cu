@@ -57,6 +57,7 @@ extern "C" int tfft_pass_supported(int log_l, int b_tile, int arith, int ept)
 
 extern "C" int tfft_launch_pass(const tfft_pass *p, void *stream)
 {
+    if (p->len) return tfft::launch_mixed(*p, (cudaStream_t)stream);
     tfft::LaunchFn f = tfft::find(p->log_l, p->b_tile, p->arith, p->ept);
     if (!f) return (int)cudaErrorInvalidValue;
     return f(*p, (cudaStream_t)stream);

@@ -323,7 +323,9 @@ __device__ __forceinline__ void finish_tile(const tfft_pass &p, const TileGeom &
         const int64_t mask = (int64_t(1) << p.tw_shift) - 1;
 #pragma unroll
         for (int q = 0; q < E; q++) {
-            const int64_t m = (t * (int64_t)(j + q * TPL)) & (p.tw_n - 1);
+            /* t < N / L and k < L, so m = t k < N needs no reduction (N
+             * need not be a power of two) */
+            const int64_t m = t * (int64_t)(j + q * TPL);
             typename A::TW w = A::tw_mul(A::load_tw(p.tw_hi, m >> p.tw_shift),
                                          A::load_tw(p.tw_lo, m & mask));
             a[q] = A::mul_tw(a[q], w);
@@ -414,6 +416,10 @@ int launch_pass(const tfft_pass &p, cudaStream_t s)
     kern<<<(unsigned)blocks, Shape<LOG_L, EPT>::TPL * B, smem, s>>>(p);
     return (int)cudaGetLastError();
 }
+
+/* lines whose length is not a power of two (fft_mixed.cuh) */
+int launch_mixed(const tfft_pass &p, cudaStream_t s);
+bool mixed_supported(int len, int b_tile, int arith);
 
 /* launch table over (log2 L, log2 B): at most 512 threads per CTA for
  * 16-byte elements (L*B <= 8192, 136 KB of shared memory) and 1024 for FP32

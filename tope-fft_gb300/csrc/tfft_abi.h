@@ -50,6 +50,8 @@ enum tfft_arith {
  *   conj_out  conjugate on store
  *   scale     multiply on store (1.0 = none; 1/N is exact for N = 2^k)
  */
+#define TFFT_MAX_RADICES 24
+
 typedef struct tfft_pass {
     int log_l;
     int b_tile;
@@ -78,7 +80,16 @@ typedef struct tfft_pass {
     /* points per thread: 0 or 16 (radix-16 stages), or 4 (radix-4 stages,
      * FP64 storage, log2 L = 2..7: small transforms) */
     int ept;
+    /* lines whose length is not a power of two: len = L (log_l unused),
+     * transformed in nrad Stockham stages of the radices radix[] (2, 3, 4,
+     * 5, 7, 8, 11, 13; product L) by the mixed-radix kernel; 0 otherwise */
+    int len;
+    int nrad;
+    unsigned char radix[TFFT_MAX_RADICES];
 } tfft_pass;
+
+/* mixed-radix lines: at most TFFT_MIXED_MAX_POINTS points per CTA (L * b_tile) */
+#define TFFT_MIXED_MAX_POINTS 4096
 
 /* ---- batches of independent transforms (persistent kernel) --------------- */
 /* one pass over one class of same-shaped transforms */
@@ -150,7 +161,8 @@ const char *tfft_error_string(int code);
 /* W_L^m = (cospi(2m/L), -sinpi(2m/L)) for m < L; arith selects double2 or
  * the double-float layout (float4: re_hi, re_lo, im_hi, im_lo). */
 int tfft_twiddle_table(void *tw, int log_l, int arith, void *stream);
-/* four-step factors: lo[m] = W_N^m (m < 2^shift), hi[h] = W_N^(h<<shift) */
+/* four-step factors: lo[m] = W_N^m (m < 2^shift), hi[h] = W_N^(h<<shift) for
+ * h < ceil(N / 2^shift); any N */
 int tfft_fourstep_tables(void *hi, void *lo, int64_t n, int shift, int arith, void *stream);
 /* rev[g] = bit reversal of g over log2n bits, g < 2^log2n */
 int tfft_bitrev_table(int *rev, int log2n, void *stream);
@@ -159,6 +171,8 @@ int tfft_bitrev_table(int *rev, int log2n, void *stream);
 int tfft_quarter_table(void *tw, int n, void *stream);
 /* W_n^m for m < n, any n (DFT path) */
 int tfft_dft_table(void *tw, int n, void *stream);
+/* W_L^m for m < L, any L, in the layout of arith (mixed-radix passes) */
+int tfft_table_any(void *tw, int len, int arith, void *stream);
 
 /* ---- tensor-core form ------------------------------------------------------ */
 /* bytes of the DFT-16 matrix table */
@@ -175,6 +189,8 @@ int tfft_tc_error(int *flag, void *stream);
 int tfft_launch_pass(const tfft_pass *p, void *stream);
 /* can this (log_l, b_tile, arith, points per thread) be launched? */
 int tfft_pass_supported(int log_l, int b_tile, int arith, int ept);
+/* can the mixed-radix kernel run lines of len points, b_tile per CTA? */
+int tfft_mixed_supported(int len, int b_tile, int arith);
 /* out[k] = sum_j in[j] W_n^{jk} (dir 1) or conjugate kernel scaled by 1/n,
  * for `rows` contiguous rows of n points */
 int tfft_launch_dft(const void *in, void *out, const void *tw, int n, int dir, int64_t rows,

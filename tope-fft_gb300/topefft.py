@@ -193,6 +193,15 @@ def _ptr(d):
     raise TypeError("unsupported data argument")
 
 
+def _need(d, x, rows, type_) -> None:
+    """A host array handed to a PlanInit must hold the data the library
+    uploads: 2 x doubles per row for C2C, x reals per row for R2C."""
+    if isinstance(d, np.ndarray):
+        want = (x if type_ == R2C else 2 * x) * rows
+        if d.size < want:
+            raise ValueError(f"data holds {d.size} values, the plan reads {want}")
+
+
 def topeFFTInit(f: TopeFFT) -> None:
     lib.topeFFTInit(C.byref(f))
 
@@ -218,10 +227,12 @@ def topeResetPassTimes(f: TopeFFT, t) -> None:
 
 
 def tope1DPlanInit(f, t, x, type_, d) -> None:
+    _need(d, x, 1, type_)
     lib.tope1DPlanInit(C.byref(f), C.byref(t), x, type_, _ptr(d))
 
 
 def tope1DBatchPlanInit(f, t, x, batch, type_, d) -> None:
+    _need(d, x, batch, type_)
     lib.tope1DBatchPlanInit(C.byref(f), C.byref(t), x, batch, type_, _ptr(d))
 
 
@@ -234,6 +245,7 @@ def tope1DDestroy(f, t) -> None:
 
 
 def tope2DPlanInit(f, t, x, y, type_, d) -> None:
+    _need(d, x, y, type_)
     lib.tope2DPlanInit(C.byref(f), C.byref(t), x, y, type_, _ptr(d))
 
 
@@ -254,6 +266,7 @@ def tope2DDestroy(f, t) -> None:
 
 
 def tope3DPlanInit(f, t, x, y, z, type_, d) -> None:
+    _need(d, x, y * z, type_)
     lib.tope3DPlanInit(C.byref(f), C.byref(t), x, y, z, type_, _ptr(d))
 
 
@@ -408,6 +421,7 @@ def pass_times(f, t):
         info = (C.c_int64 * 6)()
         lib.topePassInfo(C.byref(f), t.impl, i, info)
         out.append({"ns": int(ns[i]), "launches": int(cnt[i]), "log_l": int(info[0]),
+                    "len": (1 << int(info[0])) if info[0] >= 0 else -int(info[0]),
                     "b_tile": int(info[1]), "ctas": int(info[2]), "threads": int(info[3]),
                     "out_of_place": int(info[4]), "four_step_twiddle": int(info[5])})
     return out
