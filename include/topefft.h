@@ -28,7 +28,9 @@
  * Differences, all in the caller's favour: no assert or exit() on errors
  * (the status goes to f->error and topeGetLastError()); non-power-of-two 1D
  * lengths honour the direction (the reference's DFT kernel ignores it); 2D
- * and 3D axes of length 1 and 2 work; indexing is 64-bit.
+ * and 3D sides may be products of 2, 3, 5, 7, 11 and 13 (the reference
+ * exits on anything but powers of two); axes of length 1 and 2 work;
+ * indexing is 64-bit.
  */
 #ifndef TOPEFFT_H
 #define TOPEFFT_H

@@ -15,7 +15,8 @@ extern "C" {
 /* ---- status codes (the reference asserts instead, topefft.h:6) ---------- */
 enum topeStatus {
     TOPE_SUCCESS = 0,
-    TOPE_ERR_INVALID_SIZE = 1,   /* length not supported (e.g. 2D/3D non power of two) */
+    TOPE_ERR_INVALID_SIZE = 1,   /* length not supported (e.g. a 2D/3D side with a
+                                    prime factor above 13) */
     TOPE_ERR_INVALID_ARG = 2,    /* NULL pointer, bad direction or type */
     TOPE_ERR_ALLOC = 3,          /* device or host allocation failed */
     TOPE_ERR_CUDA = 4,           /* a CUDA call failed; see topeLastCudaError() */
@@ -69,8 +70,9 @@ void topeSync(struct topeFFT *f);
 
 /* ---- batched 1D ----------------------------------------------------------- */
 /* batch contiguous transforms of length x (row b at d + 2*b*x), any x >= 1
- * (lengths that are not powers of two run as an O(x^2) DFT below 128 points
- * and as Bluestein convolutions above).  The plan is a topePlan1D;
+ * (lengths whose prime factors are all at most 13 run as mixed-radix
+ * passes; others as an O(x^2) DFT below 128 points and as Bluestein
+ * convolutions above).  The plan is a topePlan1D;
  * tope1DExec / tope1DExecDevice / Upload / Download / Destroy apply to all
  * rows.  dataSize = 16*x*batch. */
 void tope1DBatchPlanInit(struct topeFFT *f, struct topePlan1D *t, int x, int batch, int type,
@@ -204,9 +206,9 @@ void topeHostFree(void *p);
  * next synchronising call.  impl is a plan's t->impl. */
 void topeSetPassTiming(struct topeFFT *f, int enable);
 /* Writes up to max per-pass totals (ns) and launch counts; returns the
- * plan's number of passes.  For a plan of a non-power-of-two length of 128
- * points or more these are the passes of its power-of-two sub-transforms
- * (run twice per transform), as for topePassInfo. */
+ * plan's number of passes.  For a Bluestein plan (a length of 128 points or
+ * more with a prime factor above 13) these are the passes of its
+ * sub-transforms (run twice per transform), as for topePassInfo. */
 int topePassTimes(struct topeFFT *f, void *impl, uint64_t *ns, uint64_t *launches, int max);
 void topeResetPassTimes(struct topeFFT *f, void *impl);
 /* Geometry of pass i of a plan: {log2 L (or -L for a line length L that is

@@ -69,7 +69,7 @@ def test_1d_mixed_pass_shapes(T, fw, orc):
 
 
 @pytest.mark.parametrize("n,b", [(3, 7), (60, 100), (1000, 33), (6000, 3), (4095, 2),
-                                 (100000, 2)])
+                                 (100000, 2), (400, 250), (250, 400)])
 def test_1d_mixed_batched(T, fw, orc, n, b):
     x = orc.uniform(n * b, SEED0 + 17 * n)
     for dir_ in (1, 0):
