@@ -716,7 +716,7 @@ def run_batch(args, wl: dict) -> dict:
                      "launch_us": round(ms / 2 * 1e3, 1)},
         "e2e": {"value": round(e2e_val / 1e9, 3), "unit": "GFLOP/s",
                 "h2d_bytes_per_step": nbytes,
-                "d2h_bytes_per_step": (2 * nbytes + 16 * batch) if real else 2 * nbytes,
+                "d2h_bytes_per_step": 2 * nbytes,
                 "ms_per_step": round(e2e_ms, 3)},
         "gpu_launches": 2 * args.steps,
         "clocks": clocks,

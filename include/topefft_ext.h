@@ -123,7 +123,10 @@ void tope3DUploadSpectrum(struct topeFFT *f, struct topePlan3D *t, const double 
  *     synchronous Exec as TOPE_ERR_TIMEOUT.
  * The FP64 Exec/Upload/Download entry points reject these plans (and the
  * F32 ones reject FP64 plans) with TOPE_ERR_INVALID_ARG.  Device-resident
- * execution uses tope*DExecDevice. */
+ * execution uses tope*DExecDevice.
+ * type = R2C works as for FP64 (x + 2 floats per row of output); the
+ * real-data steps around the half-length complex transform run in
+ * double-float and round once, in every split mode. */
 enum topeSplitMode { TOPE_SPLIT_ACCURATE = 0, TOPE_SPLIT_FAST = 1, TOPE_SPLIT_TENSOR = 2 };
 void topeSetSplitMode(struct topeFFT *f, int mode);
 void tope1DBatchPlanInitF32(struct topeFFT *f, struct topePlan1D *t, int x, int batch, int type,
@@ -137,6 +140,9 @@ void tope3DExecF32(struct topeFFT *f, struct topePlan3D *t, float *d, int dir);
 /* impl is the plan's t->impl */
 void topeUploadF32(struct topeFFT *f, void *impl, const float *d);
 void topeDownloadF32(struct topeFFT *f, void *impl, float *d);
+/* the spectrum of an FP32 R2C plan (x/2 + 1 complex floats per row), for an
+ * inverse, as tope{1,2,3}DUploadSpectrum */
+void topeUploadSpectrumF32(struct topeFFT *f, void *impl, const float *spec);
 
 /* ---- batches of independent transforms of uneven sizes ------------------ */
 /* count transforms packed back to back in one buffer, transform i of

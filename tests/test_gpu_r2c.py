@@ -104,12 +104,10 @@ def test_r2c_device_resident_chain(T, fw, orc):
     T.tope1DDestroy(fw, t)
 
 
-def test_r2c_rejects_bad_shapes_and_split_precision(T, fw):
+def test_r2c_rejects_bad_shapes(T, fw):
     t = T.TopePlan1D()
     T.tope1DPlanInit(fw, t, 7, T.R2C, np.zeros(16))
     assert fw.error == T.TOPE_ERR_INVALID_SIZE and not t.impl
-    T.tope1DBatchPlanInitF32(fw, t, 64, 1, T.R2C, np.zeros(130, dtype=np.float32))
-    assert fw.error == T.TOPE_ERR_UNSUPPORTED and not t.impl
     t2 = T.TopePlan2D()
     T.tope2DPlanInit(fw, t2, 7, 8, T.R2C, np.zeros(128))  # odd x
     assert fw.error == T.TOPE_ERR_INVALID_SIZE and not t2.impl
@@ -189,3 +187,55 @@ def test_c2r_nd_from_uploaded_spectrum(T, fw, orc, dims):
         T.tope2DExecX(fw, t)
         assert fw.error == T.TOPE_ERR_UNSUPPORTED
     destroy_nd(T, fw, t)
+
+
+# ---------------------------------------------------------------- FP32 storage
+SPLIT_GATES = {"accurate": 1e-7, "fast": 2.5e-7, "tensor": 5e-7}
+SPLIT_CASES = [((4096, 1, 1), 1), ((1 << 20, 1, 1), 1), ((64, 1, 1), 33), ((1 << 14, 1, 1), 64),
+               ((1000, 1, 1), 8), ((256, 128, 1), 1), ((64, 32, 16), 1), ((100, 60, 1), 1)]
+
+
+@pytest.mark.parametrize("mode", ["accurate", "fast", "tensor"])
+@pytest.mark.parametrize("dims,batch", SPLIT_CASES, ids=lambda v: str(v))
+def test_r2c_split_precision(T, orc, mode, dims, batch):
+    """R2C/C2R with FP32 storage in each split mode, against the FP64 oracle
+    of the unrounded reals; the spectrum uploaded back gives the reals."""
+    nx, ny, nz = dims
+    if mode == "tensor" and any(v & (v - 1) for v in (nx // 2, ny, nz)):
+        pytest.skip("the tensor form runs power-of-two lines only")
+    gate = SPLIT_GATES[mode]
+    f = T.TopeFFT()
+    T.topeFFTInit(f)
+    T.topeSetSplitMode(f, {"accurate": 0, "fast": 1, "tensor": 2}[mode])
+    n = nx * ny * nz
+    xr = orc.uniform(n * batch // 2, SEED0 + 31 + nx)
+    d = np.zeros((nx + 2) * ny * nz * batch, dtype=np.float32)
+    d[:n * batch] = xr
+    if ny == 1 and nz == 1:
+        t = T.TopePlan1D()
+        T.tope1DBatchPlanInitF32(f, t, nx, batch, T.R2C, d)
+        want = oracle_spectrum(orc, xr, nx, batch)
+    elif nz == 1:
+        t = T.TopePlan2D()
+        T.tope2DPlanInitF32(f, t, nx, ny, T.R2C, d)
+        want = oracle_spectrum_nd(orc, xr, dims)
+    else:
+        t = T.TopePlan3D()
+        T.tope3DPlanInitF32(f, t, nx, ny, nz, T.R2C, d)
+        want = oracle_spectrum_nd(orc, xr, dims)
+    T.check(f)
+    T.execF32(f, t, d, T.FORWARD)
+    T.check(f)
+    assert orc.rel_l2(d.astype(np.float64), want) <= gate
+    T.execF32(f, t, d, T.INVERSE)
+    T.check(f)
+    assert orc.rel_l2(d[:n * batch].astype(np.float64), xr) <= gate
+    T.upload_spectrum(f, t, want.astype(np.float32))
+    T.check(f)
+    back = np.zeros_like(d)
+    T.execF32(f, t, back, T.INVERSE)
+    T.check(f)
+    assert orc.rel_l2(back[:n * batch].astype(np.float64), xr) <= gate
+    {T.TopePlan1D: T.tope1DDestroy, T.TopePlan2D: T.tope2DDestroy,
+     T.TopePlan3D: T.tope3DDestroy}[type(t)](f, t)
+    T.topeFFTDestroy(f)

@@ -296,7 +296,7 @@ __global__ void k_bluestein_post(const double2 *__restrict__ w, const double2 *_
 /* real-data transforms of length n = 2m through a complex transform of
  * length m: lo[i] = W_n^i (i < 2^shift), hi[h] = W_n^(h << shift) (h <= m >> shift),
  * angles from the exact ratio (i mod n)/n, one rounding each */
-__global__ void k_real_tables(double2 *hi, double2 *lo, int64_t n, int shift, int64_t nhi)
+__global__ void k_real_tables(void *hi, void *lo, int64_t n, int shift, int64_t nhi, int arith)
 {
     const int64_t nlo = int64_t(1) << shift;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nlo + nhi;
@@ -304,8 +304,8 @@ __global__ void k_real_tables(double2 *hi, double2 *lo, int64_t n, int shift, in
         const int64_t e = i < nlo ? i : (i - nlo) << shift;
         double s, c;
         sincospi(2.0 * (double)(e % n) / (double)n, &s, &c);
-        if (i < nlo) lo[i] = make_double2(c, -s);
-        else hi[i - nlo] = make_double2(c, -s);
+        put_tw(i < nlo ? lo : hi, i < nlo ? i : i - nlo, make_double2(c, -s),
+               arith == TFFT_ARITH_F64 || arith == TFFT_ARITH_DF64 ? TFFT_ARITH_F64 : arith);
     }
 }
 
@@ -351,6 +351,61 @@ __global__ void k_c2r_pre(const double2 *__restrict__ x, double2 *__restrict__ z
         w.y = -w.y;
         const double2 o = cmul(make_double2(0.5 * (a.x - b.x), 0.5 * (a.y - b.y)), w);
         z[i] = make_double2(e.x - o.y, e.y + o.x);
+    }
+}
+
+/* The same two steps for FP32 storage (the split-precision forms): the
+ * loads are exact in double-float, E, O and W_n^k O are formed in
+ * double-float with W_n^k from (hi, lo) float pair tables, and each output
+ * rounds once to FP32.  A = ArithDF32. */
+using DF = tfft::ArithDF32;
+
+__device__ __forceinline__ DF::C df_half(DF::C v)
+{
+    v.r.h *= 0.5f;
+    v.r.l *= 0.5f;
+    v.i.h *= 0.5f;
+    v.i.l *= 0.5f;
+    return v;
+}
+
+__device__ __forceinline__ DF::TW w_real32(const float4 *hi, const float4 *lo, int shift, int64_t k)
+{
+    return DF::tw_mul(__ldg(hi + (k >> shift)), __ldg(lo + (k & ((int64_t(1) << shift) - 1))));
+}
+
+__global__ void k_r2c_post32(const float2 *__restrict__ z, float2 *__restrict__ x,
+                             const float4 *__restrict__ hi, const float4 *__restrict__ lo, int shift,
+                             int64_t m, int64_t rows)
+{
+    const int64_t per = m + 1;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < per * rows;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = i / per, k = i - r * per;
+        const DF::C a = DF::load_s(z[r * m + (k == m ? 0 : k)], 0);
+        const DF::C b = DF::conj(DF::load_s(z[r * m + (k == 0 ? 0 : m - k)], 0));
+        const DF::C e = df_half(DF::add(a, b));
+        const DF::C o = df_half(DF::mul_mi(DF::sub(a, b))); /* (a - b) / (2i) */
+        x[i] = DF::store_s(DF::add(e, DF::mul_tw(o, w_real32(hi, lo, shift, k))), 0, 1.0);
+    }
+}
+
+__global__ void k_c2r_pre32(const float2 *__restrict__ x, float2 *__restrict__ z,
+                            const float4 *__restrict__ hi, const float4 *__restrict__ lo, int shift,
+                            int64_t m, int64_t rows)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m * rows;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = i / m, k = i - r * m;
+        const DF::C a = DF::load_s(x[r * (m + 1) + k], 0);
+        const DF::C b = DF::conj(DF::load_s(x[r * (m + 1) + m - k], 0));
+        const DF::C e = df_half(DF::add(a, b));
+        float4 w = w_real32(hi, lo, shift, k);
+        w.z = -w.z;
+        w.w = -w.w;
+        const DF::C o = df_half(DF::mul_tw(DF::sub(a, b), w));
+        /* z = e + i o */
+        z[i] = DF::store_s(DF::sub(e, DF::mul_mi(o)), 0, 1.0);
     }
 }
 
@@ -470,27 +525,37 @@ int tfft_bluestein_post(const void *w, const void *chirp, void *x, int64_t n, in
     return (int)cudaGetLastError();
 }
 
-int tfft_real_tables(void *hi, void *lo, int64_t n, int shift, void *s)
+int tfft_real_tables(void *hi, void *lo, int64_t n, int shift, int arith, void *s)
 {
     const int64_t nhi = ((n / 2) >> shift) + 1;
     k_real_tables<<<grid_for((int64_t(1) << shift) + nhi, 256), 256, 0, (cudaStream_t)s>>>(
-        (double2 *)hi, (double2 *)lo, n, shift, nhi);
+        hi, lo, n, shift, nhi, arith);
     return (int)cudaGetLastError();
 }
 
 int tfft_r2c_post(const void *z, void *x, const void *hi, const void *lo, int shift, int64_t m,
-                  int64_t rows, void *s)
+                  int64_t rows, int arith, void *s)
 {
-    k_r2c_post<<<grid_for((m + 1) * rows, 256), 256, 0, (cudaStream_t)s>>>(
-        (const double2 *)z, (double2 *)x, (const double2 *)hi, (const double2 *)lo, shift, m, rows);
+    if (TFFT_ELEM_BYTES(arith) == 8)
+        k_r2c_post32<<<grid_for((m + 1) * rows, 256), 256, 0, (cudaStream_t)s>>>(
+            (const float2 *)z, (float2 *)x, (const float4 *)hi, (const float4 *)lo, shift, m, rows);
+    else
+        k_r2c_post<<<grid_for((m + 1) * rows, 256), 256, 0, (cudaStream_t)s>>>(
+            (const double2 *)z, (double2 *)x, (const double2 *)hi, (const double2 *)lo, shift, m,
+            rows);
     return (int)cudaGetLastError();
 }
 
 int tfft_c2r_pre(const void *x, void *z, const void *hi, const void *lo, int shift, int64_t m,
-                 int64_t rows, void *s)
+                 int64_t rows, int arith, void *s)
 {
-    k_c2r_pre<<<grid_for(m * rows, 256), 256, 0, (cudaStream_t)s>>>(
-        (const double2 *)x, (double2 *)z, (const double2 *)hi, (const double2 *)lo, shift, m, rows);
+    if (TFFT_ELEM_BYTES(arith) == 8)
+        k_c2r_pre32<<<grid_for(m * rows, 256), 256, 0, (cudaStream_t)s>>>(
+            (const float2 *)x, (float2 *)z, (const float4 *)hi, (const float4 *)lo, shift, m, rows);
+    else
+        k_c2r_pre<<<grid_for(m * rows, 256), 256, 0, (cudaStream_t)s>>>(
+            (const double2 *)x, (double2 *)z, (const double2 *)hi, (const double2 *)lo, shift, m,
+            rows);
     return (int)cudaGetLastError();
 }
 

@@ -219,16 +219,18 @@ int tfft_bluestein_post(const void *w, const void *chirp, void *x, int64_t n, in
                         int conj_out, double scale, int64_t rows, void *stream);
 
 /* Real-data transforms of even length n = 2m through a complex transform of
- * length m over the same bytes (FP64):
+ * length m over the same bytes, in the storage of arith (FP64 for
+ * TFFT_ARITH_F64/DF64, FP32 for the split-precision forms, whose tables are
+ * (hi, lo) float pairs and whose steps run in double-float):
  *   tables:   lo[i] = W_n^i (i < 2^shift), hi[h] = W_n^(h << shift), h <= m >> shift;
  *   r2c_post: z = FFT_m of the packed reals, row by row (m complex) -> the
  *             m + 1 non-redundant outputs x[0..m] of each row;
  *   c2r_pre:  x[0..m] per row -> z, whose inverse FFT_m is the packed reals. */
-int tfft_real_tables(void *hi, void *lo, int64_t n, int shift, void *stream);
+int tfft_real_tables(void *hi, void *lo, int64_t n, int shift, int arith, void *stream);
 int tfft_r2c_post(const void *z, void *x, const void *hi, const void *lo, int shift, int64_t m,
-                  int64_t rows, void *stream);
+                  int64_t rows, int arith, void *stream);
 int tfft_c2r_pre(const void *x, void *z, const void *hi, const void *lo, int shift, int64_t m,
-                 int64_t rows, void *stream);
+                 int64_t rows, int arith, void *stream);
 
 #ifdef __cplusplus
 }

@@ -804,7 +804,7 @@ static int impl_create(struct topeFFT *f, tope_impl **out, int ndim, int64_t x, 
     const int fp64_io = P->es == 16;
     P->real = real == IMPL_REAL;
     const int spec = real == IMPL_SPEC;
-    if ((P->real && ndim != 1) || (real && !fp64_io)) {
+    if (P->real && ndim != 1) {
         impl_free(P);
         return set_status(f, TOPE_ERR_UNSUPPORTED);
     }
@@ -910,10 +910,10 @@ static int impl_create(struct topeFFT *f, tope_impl **out, int ndim, int64_t x, 
         while (((int64_t)1 << (2 * shift)) < 2 * x) shift++;
         P->rtw_shift = shift;
         const size_t nhi = (size_t)(x >> shift) + 1;
-        if (tfft_malloc(&P->spec, 16 * (size_t)(x + 1) * (size_t)batch) ||
+        if (tfft_malloc(&P->spec, (size_t)P->es * (size_t)(x + 1) * (size_t)batch) ||
             tfft_malloc(&P->rtw_hi, 16 * nhi) || tfft_malloc(&P->rtw_lo, (size_t)16 << shift))
             st = set_status(f, TOPE_ERR_ALLOC);
-        else if ((rc = tfft_real_tables(P->rtw_hi, P->rtw_lo, 2 * x, shift, stream)))
+        else if ((rc = tfft_real_tables(P->rtw_hi, P->rtw_lo, 2 * x, shift, P->arith, stream)))
             st = cuda_status(f, rc);
     }
     tfft_event_record(P->kev.b, stream);
@@ -1035,7 +1035,7 @@ static int impl_exec_async(struct topeFFT *f, tope_impl *P, int dir, int hold)
         }
         /* spectrum -> packed spectrum of the half-length transform */
         if (!st && (rc = tfft_c2r_pre(spec_buf(P), P->buf[P->cur], P->rtw_hi, P->rtw_lo,
-                                      P->rtw_shift, m, rows, stream)))
+                                      P->rtw_shift, m, rows, P->arith, stream)))
             st = cuda_status(f, rc);
         P->spec_cur = 0;
     }
@@ -1073,7 +1073,7 @@ static int impl_exec_async(struct topeFFT *f, tope_impl *P, int dir, int hold)
     }
     if (!st && P->real && dir == FORWARD) {
         if ((rc = tfft_r2c_post(P->buf[P->cur], spec_buf(P), P->rtw_hi, P->rtw_lo, P->rtw_shift,
-                                m, rows, stream)))
+                                m, rows, P->arith, stream)))
             st = cuda_status(f, rc);
         /* 2D/3D: then the forward along y (and z) on the spectrum */
         if (!st && P->specp) st = run_passes(f, P->specp, 0, P->specp->npass, FORWARD, 1.0);
@@ -1091,7 +1091,7 @@ static int impl_exec_async(struct topeFFT *f, tope_impl *P, int dir, int hold)
 static void *cur_data(const tope_impl *P, size_t *bytes)
 {
     if (P->real && P->spec_cur) {
-        *bytes = (size_t)16 * (size_t)(P->c[0] + 1) * (size_t)P->c[3];
+        *bytes = (size_t)P->es * (size_t)(P->c[0] + 1) * (size_t)P->c[3];
         return spec_buf(P);
     }
     *bytes = (size_t)P->total * P->es;
@@ -1455,17 +1455,18 @@ void tope1DDownload(struct topeFFT *f, struct topePlan1D *t, double *d)
     if (P) impl_download(f, P, d, 16, &t->totalKernel, &t->totalMemory);
 }
 
-static void impl_upload_spectrum(struct topeFFT *f, tope_impl *P, const double *spec,
+/* es_caller: the element size of the calling entry point (16 FP64, 8 FP32) */
+static void impl_upload_spectrum(struct topeFFT *f, tope_impl *P, const void *spec, int es_caller,
                                  uint64_t *t_mem)
 {
-    if (!P->real || !spec) {
+    if (!P->real || !spec || P->es != es_caller) {
         set_status(f, TOPE_ERR_INVALID_ARG);
         return;
     }
     void *stream = f->command_queue;
     tfft_event_record(P->mev.a, stream);
-    int rc = tfft_h2d(spec_buf(P), spec, (size_t)16 * (size_t)(P->c[0] + 1) * (size_t)P->c[3],
-                      stream);
+    int rc = tfft_h2d(spec_buf(P), spec,
+                      (size_t)P->es * (size_t)(P->c[0] + 1) * (size_t)P->c[3], stream);
     tfft_event_record(P->mev.b, stream);
     if (!rc) rc = tfft_stream_sync(stream);
     if (rc) {
@@ -1482,19 +1483,19 @@ static void impl_upload_spectrum(struct topeFFT *f, tope_impl *P, const double *
 void tope1DUploadSpectrum(struct topeFFT *f, struct topePlan1D *t, const double *spec)
 {
     tope_impl *P = t ? impl_of(f, t->impl) : NULL;
-    if (P) impl_upload_spectrum(f, P, spec, &t->totalMemory);
+    if (P) impl_upload_spectrum(f, P, spec, 16, &t->totalMemory);
 }
 
 void tope2DUploadSpectrum(struct topeFFT *f, struct topePlan2D *t, const double *spec)
 {
     tope_impl *P = t ? impl_of(f, t->impl) : NULL;
-    if (P) impl_upload_spectrum(f, P, spec, &t->totalMemory);
+    if (P) impl_upload_spectrum(f, P, spec, 16, &t->totalMemory);
 }
 
 void tope3DUploadSpectrum(struct topeFFT *f, struct topePlan3D *t, const double *spec)
 {
     tope_impl *P = t ? impl_of(f, t->impl) : NULL;
-    if (P) impl_upload_spectrum(f, P, spec, &t->totalMemory);
+    if (P) impl_upload_spectrum(f, P, spec, 16, &t->totalMemory);
 }
 
 void tope1DDestroy(struct topeFFT *f, struct topePlan1D *t)
@@ -1553,7 +1554,7 @@ static void plan2d(struct topeFFT *f, struct topePlan2D *t, int x, int y, int ty
         if (real_nd_create(f, &P, 2, x, y, 1, d, arith, &t->totalPreKernel, &t->totalMemory))
             return;
         t->impl = P;
-        t->dataSize = (size_t)8 * (size_t)x * (size_t)y;
+        t->dataSize = (size_t)(P->es / 2) * (size_t)x * (size_t)y;
         t->data = P->buf[P->cur];
         return;
     }
@@ -1676,7 +1677,7 @@ static void plan3d(struct topeFFT *f, struct topePlan3D *t, int x, int y, int z,
         if (real_nd_create(f, &P, 3, x, y, z, d, arith, &t->totalPreKernel, &t->totalMemory))
             return;
         t->impl = P;
-        t->dataSize = (size_t)8 * (size_t)x * (size_t)y * (size_t)z;
+        t->dataSize = (size_t)(P->es / 2) * (size_t)x * (size_t)y * (size_t)z;
         t->data = P->buf[P->cur];
         return;
     }
@@ -1735,6 +1736,13 @@ void topeUploadF32(struct topeFFT *f, void *impl, const float *d)
     tope_impl *P = impl_of(f, impl);
     uint64_t ns = 0;
     if (P) impl_upload(f, P, d, 8, &ns);
+}
+
+void topeUploadSpectrumF32(struct topeFFT *f, void *impl, const float *spec)
+{
+    tope_impl *P = impl_of(f, impl);
+    uint64_t ns = 0;
+    if (P) impl_upload_spectrum(f, P, spec, 8, &ns);
 }
 
 void topeDownloadF32(struct topeFFT *f, void *impl, float *d)

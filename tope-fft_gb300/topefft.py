@@ -153,6 +153,7 @@ SIGNATURES = [
     ("tope3DExecF32", None, [_F, _P3, _FL, C.c_int]),
     ("topeUploadF32", None, [_F, _vp, _FL]),
     ("topeDownloadF32", None, [_F, _vp, _FL]),
+    ("topeUploadSpectrumF32", None, [_F, _vp, _FL]),
     ("topeSetSplitMode", None, [_F, C.c_int]),
     ("topeBatchPlanInit", None, [_F, _PB, C.c_int, _IP, _IP, C.c_int, _D]),
     ("topeBatchPlanInitF32", None, [_F, _PB, C.c_int, _IP, _IP, C.c_int, _FL]),
@@ -313,7 +314,11 @@ def download(f, t, d) -> None:
 
 
 def upload_spectrum(f, t, spec) -> None:
-    """R2C plans: the x/2 + 1 complex outputs per row, for an inverse."""
+    """R2C plans: the x/2 + 1 complex outputs per row, for an inverse
+    (a float32 array for the split-precision plans)."""
+    if isinstance(spec, np.ndarray) and spec.dtype == np.float32:
+        lib.topeUploadSpectrumF32(C.byref(f), t.impl, _fptr(spec))
+        return
     fn = {TopePlan1D: lib.tope1DUploadSpectrum, TopePlan2D: lib.tope2DUploadSpectrum,
           TopePlan3D: lib.tope3DUploadSpectrum}[type(t)]
     fn(C.byref(f), C.byref(t), _ptr(spec))
@@ -344,14 +349,17 @@ def _fptr(d):
 
 
 def tope1DBatchPlanInitF32(f, t, x, batch, type_, d) -> None:
+    _need(d, x, batch, type_)
     lib.tope1DBatchPlanInitF32(C.byref(f), C.byref(t), x, batch, type_, _fptr(d))
 
 
 def tope2DPlanInitF32(f, t, x, y, type_, d) -> None:
+    _need(d, x, y, type_)
     lib.tope2DPlanInitF32(C.byref(f), C.byref(t), x, y, type_, _fptr(d))
 
 
 def tope3DPlanInitF32(f, t, x, y, z, type_, d) -> None:
+    _need(d, x, y * z, type_)
     lib.tope3DPlanInitF32(C.byref(f), C.byref(t), x, y, z, type_, _fptr(d))
 
 
