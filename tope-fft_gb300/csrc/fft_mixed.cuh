@@ -230,8 +230,9 @@ __global__ void __launch_bounds__(kMixedThreads, pass_min_blocks<A, kMixedThread
         if (p.post_tw) {
             const int64_t t = p.tw_level == 0 ? g0 : g1;
             const int64_t m = t * (int64_t)i; /* < N: no reduction needed */
-            v = A::mul_tw(v, A::tw_mul(A::load_tw(p.tw_hi, m >> p.tw_shift),
-                                       A::load_tw(p.tw_lo, m & mask)));
+            v = A::mul_tw(v, p.tw_lo ? A::tw_mul(A::load_tw(p.tw_hi, m >> p.tw_shift),
+                                                 A::load_tw(p.tw_lo, m & mask))
+                                     : A::load_tw(p.tw_hi, m));
         }
         if (p.conj_out) v = A::conj(v);
         __stcs(out + obase + g0 * p.os[0] + (int64_t)i * p.oes, A::store_s(v, delta_out, p.scale));

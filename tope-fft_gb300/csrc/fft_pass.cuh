@@ -326,8 +326,10 @@ __device__ __forceinline__ void finish_tile(const tfft_pass &p, const TileGeom &
             /* t < N / L and k < L, so m = t k < N needs no reduction (N
              * need not be a power of two) */
             const int64_t m = t * (int64_t)(j + q * TPL);
-            typename A::TW w = A::tw_mul(A::load_tw(p.tw_hi, m >> p.tw_shift),
-                                         A::load_tw(p.tw_lo, m & mask));
+            /* tw_lo NULL: tw_hi is the whole table W_N^m, m < N */
+            typename A::TW w = p.tw_lo ? A::tw_mul(A::load_tw(p.tw_hi, m >> p.tw_shift),
+                                                   A::load_tw(p.tw_lo, m & mask))
+                                       : A::load_tw(p.tw_hi, m);
             a[q] = A::mul_tw(a[q], w);
         }
     }

@@ -46,7 +46,8 @@ enum tfft_arith {
  *   conj_in   conjugate on load (inverse transforms run as conj(F(conj x)))
  *   post_tw   multiply output element k of a line by W_N^{t*k}, where t is
  *             g0 (tw_level 0) or g1 (tw_level 1) and N = tw_n; the factor is
- *             tw_hi[m >> tw_shift] * tw_lo[m & (2^tw_shift - 1)], m = t*k mod N
+ *             tw_hi[m >> tw_shift] * tw_lo[m & (2^tw_shift - 1)], m = t*k < N,
+ *             or tw_hi[m] when tw_lo is NULL (a whole table of N entries)
  *   conj_out  conjugate on store
  *   scale     multiply on store (1.0 = none; 1/N is exact for N = 2^k)
  */

@@ -374,6 +374,10 @@ static int mixed_radices(int64_t len, unsigned char *radix)
     return len == 1 ? n : -1;
 }
 
+/* four-step factors of at most this many points come from one whole table
+ * of W_N (16 N bytes) in FP64 plans */
+#define FULL_TW_MAX ((int64_t)1 << 24)
+
 /* lines per CTA of a mixed-radix pass: a power of two (at most 256) with
  * about 2048 points per CTA (4096 for lines longer than 2048) */
 static int choose_b_mixed(int64_t len, int64_t n0)
@@ -388,7 +392,7 @@ static int choose_b_mixed(int64_t len, int64_t n0)
 /* W_L table of a mixed-radix pass of length L */
 static int impl_mixed_table(struct topeFFT *f, tope_impl *P, int64_t len, const void **out)
 {
-    int key = (1 << 24) | (int)(len << 3) | P->arith;
+    int key = -2 - (int)(len * 8 + P->arith); /* below the four-step tables' -1 */
     for (int i = 0; i < P->ntabs; i++)
         if (P->tab_key[i] == key) {
             *out = P->tabs[i];
@@ -487,7 +491,21 @@ static int add_pass(struct topeFFT *f, tope_impl *P, int64_t len, int64_t ies, i
         p->mma_b = P->tc_matrix;
     }
     p->b_tile = b;
-    if (post_tw) {
+    if (post_tw && P->arith == TFFT_ARITH_F64 && tw_n <= FULL_TW_MAX) {
+        /* FP64 butterflies: one load from the whole table W_N^m instead of
+         * the product of two table entries saves 4 of the pass's ~45 FP64
+         * instructions per point (the FP64 pipe bounds this path) */
+        const void *full;
+        const int lgn = ilog2_exact64(tw_n);
+        int st = lgn >= 0 ? impl_wl_table(f, P, lgn, &full) : impl_mixed_table(f, P, tw_n, &full);
+        if (st) return st;
+        p->post_tw = 1;
+        p->tw_level = lvl_tw;
+        p->tw_shift = 0;
+        p->tw_n = tw_n;
+        p->tw_hi = full;
+        p->tw_lo = NULL;
+    } else if (post_tw) {
         /* two-level table of W_N^m: 2^shift low entries, ceil(N / 2^shift)
          * high ones */
         int lgn = 0;
