@@ -375,8 +375,10 @@ static int mixed_radices(int64_t len, unsigned char *radix)
 }
 
 /* four-step factors of at most this many points come from one whole table
- * of W_N (16 N bytes) in FP64 plans */
-#define FULL_TW_MAX ((int64_t)1 << 24)
+ * of W_N (16 N bytes, at most 64 MB, which stays in the 129 MB L2) in FP64
+ * plans; at 2^24 points a 256 MB table read at scattered indices gained
+ * under 1% for 50% more memory */
+#define FULL_TW_MAX ((int64_t)1 << 22)
 
 /* lines per CTA of a mixed-radix pass: a power of two (at most 256) with
  * about 2048 points per CTA (4096 for lines longer than 2048) */
