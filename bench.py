@@ -207,7 +207,7 @@ def measured_peaks() -> tuple[float, str]:
 def ncu_traffic(workload: str, arith: str):
     """Per-launch DRAM bytes of the dominant kernel from the committed ncu
     summary for this workload (profiles/*.txt line 'traffic_bytes_per_launch:')."""
-    for p in sorted((ROOT / "profiles").glob(f"*pass_kernel_{arith}_{workload}.txt")):
+    for p in sorted((ROOT / "profiles").glob(f"*_kernel_{arith}_{workload}.txt")):
         for line in p.read_text().splitlines():
             if line.startswith("traffic_bytes_per_launch:"):
                 try:
