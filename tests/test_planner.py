@@ -1,0 +1,145 @@
+"""The host planner on the CPU.  topefft.c and batch.c are linked with a
+host-only stand-in for the CUDA side (tests/drivers/abi_stub.c): plans are
+built through the public entry points and their pass structure is read back
+with topePassInfo, with no GPU.  Covers the decisions the GPU tests rely on:
+one pass or a four-step split, three-pass lines, the small-transform shape,
+mixed-radix splits, the Bluestein sub-transform size, real-data row plans and
+the tensor form's tiles."""
+import ctypes as C
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+
+@pytest.fixture(scope="module")
+def S(T, tmp_path_factory):
+    out = tmp_path_factory.mktemp("stub") / "libtopefft_stub.so"
+    csrc = ROOT / "tope-fft_gb300" / "csrc"
+    subprocess.run(["gcc", "-O1", "-fPIC", "-shared", "-std=gnu11", f"-I{csrc}",
+                    f"-I{ROOT / 'include'}", str(csrc / "topefft.c"), str(csrc / "batch.c"),
+                    str(ROOT / "tests" / "drivers" / "abi_stub.c"), "-o", str(out)], check=True)
+    return T.load_library(out)
+
+
+@pytest.fixture
+def fw(T, S):
+    f = T.TopeFFT()
+    S.topeFFTInit(C.byref(f))
+    assert f.error == T.TOPE_SUCCESS
+    yield f
+    S.topeFFTDestroy(C.byref(f))
+
+
+def passes(S, f, t):
+    n = S.topePassTimes(C.byref(f), t.impl, None, None, 0)
+    info = (C.c_int64 * 6)()
+    out = []
+    for i in range(n):
+        assert S.topePassInfo(C.byref(f), t.impl, i, info) == 0
+        out.append({"len": (1 << info[0]) if info[0] >= 0 else -info[0], "b": info[1],
+                    "ctas": info[2], "threads": info[3], "oop": info[4], "tw": info[5]})
+    return out
+
+
+def plan1d(T, S, f, n, batch=1, real=False, f32=False):
+    t = T.TopePlan1D()
+    fn = S.tope1DBatchPlanInitF32 if f32 else S.tope1DBatchPlanInit
+    fn(C.byref(f), C.byref(t), n, batch, T.R2C if real else T.C2C, None)
+    return t
+
+
+@pytest.mark.parametrize("n,lens,tw,oop", [
+    (1 << 20, [1024, 1024], [1, 0], [0, 1]),
+    (1 << 27, [512, 512, 512], [1, 1, 0], [0, 0, 1]),
+    (10 ** 6, [1000, 1000], [1, 0], [0, 1]),
+    (4096, [64, 64], [1, 0], [0, 1]),
+    (1001, [1001], [0], [0]),
+    (6000, [80, 75], [1, 0], [0, 1]),
+    (2048 * 3, [64, 96], [1, 0], [0, 1]),
+])
+def test_1d_pass_structure(T, S, fw, n, lens, tw, oop):
+    t = plan1d(T, S, fw, n)
+    assert fw.error == T.TOPE_SUCCESS
+    p = passes(S, fw, t)
+    assert [q["len"] for q in p] == lens
+    assert [q["tw"] for q in p] == tw
+    assert [q["oop"] for q in p] == oop
+    S.tope1DDestroy(C.byref(fw), C.byref(t))
+
+
+def test_small_transform_runs_4_points_per_thread(T, S, fw):
+    """A lone 4096-point line: two passes of 64-point lines, 32 CTAs of 32
+    threads (4 points per thread); batched, one 4096-point pass."""
+    p = passes(S, fw, plan1d(T, S, fw, 4096))
+    assert [(q["b"], q["ctas"], q["threads"]) for q in p] == [(2, 32, 32), (2, 32, 32)]
+    p = passes(S, fw, plan1d(T, S, fw, 4096, batch=64))
+    assert [q["len"] for q in p] == [4096] and p[0]["threads"] == 256
+
+
+@pytest.mark.parametrize("n", [12288, 3 ** 16, 5 ** 9, 2 * 3 * 5 * 7 * 11 * 13 * 16])
+def test_mixed_splits(T, S, fw, n):
+    """Every pass fits one CTA (<= 4096 points, or a power of two <= 2^13) and
+    the pass lengths multiply to n."""
+    p = passes(S, fw, plan1d(T, S, fw, n))
+    assert fw.error == T.TOPE_SUCCESS
+    assert int(np.prod([q["len"] for q in p])) == n
+    for q in p:
+        L = q["len"]
+        assert (L & (L - 1) == 0 and L <= 8192) or L <= 4096
+    assert len(p) == (3 if n > 4096 * 4096 else 2)
+
+
+@pytest.mark.parametrize("n,m", [(131, 270), (10007, 32768), (17 * 1031, 35280),
+                                 (999983, 1 << 21)])
+def test_bluestein_sub_transform_size(T, S, fw, n, m):
+    p = passes(S, fw, plan1d(T, S, fw, n))
+    assert int(np.prod([q["len"] for q in p])) == m
+
+
+def test_small_primes_use_the_dft(T, S, fw):
+    t = plan1d(T, S, fw, 127)
+    assert fw.error == T.TOPE_SUCCESS and passes(S, fw, t) == []
+
+
+@pytest.mark.parametrize("dims,lens", [((100, 60, 1), [100, 60]), ((30, 20, 50), [30, 20, 50]),
+                                       ((1 << 14, 4, 1), [128, 128, 4])])
+def test_nd_pass_structure(T, S, fw, dims, lens):
+    nx, ny, nz = dims
+    if nz == 1:
+        t = T.TopePlan2D()
+        S.tope2DPlanInit(C.byref(fw), C.byref(t), nx, ny, T.C2C, None)
+    else:
+        t = T.TopePlan3D()
+        S.tope3DPlanInit(C.byref(fw), C.byref(t), nx, ny, nz, T.C2C, None)
+    assert fw.error == T.TOPE_SUCCESS
+    assert [q["len"] for q in passes(S, fw, t)] == lens
+
+
+def test_nd_rejects_large_prime_sides(T, S, fw):
+    t = T.TopePlan2D()
+    S.tope2DPlanInit(C.byref(fw), C.byref(t), 17, 8, T.C2C, None)
+    assert fw.error == T.TOPE_ERR_INVALID_SIZE and not t.impl
+
+
+def test_real_plans_transform_half_length_rows(T, S, fw):
+    p = passes(S, fw, plan1d(T, S, fw, 2000, real=True))
+    assert [q["len"] for q in p] == [1000]
+    t = T.TopePlan2D()
+    S.tope2DPlanInit(C.byref(fw), C.byref(t), 100, 60, T.R2C, None)
+    assert fw.error == T.TOPE_SUCCESS
+    assert [q["len"] for q in passes(S, fw, t)] == [50]
+
+
+def test_split_precision_shapes(T, S, fw):
+    """FP32 storage takes 2^14-point lines in one pass, so 2^29 points are three
+    passes; the tensor form uses its fixed tiles and rejects mixed radix."""
+    p = passes(S, fw, plan1d(T, S, fw, 1 << 29, f32=True))
+    assert [q["len"] for q in p] == [1024, 1024, 512]
+    S.topeSetSplitMode(C.byref(fw), 2)
+    p = passes(S, fw, plan1d(T, S, fw, 1 << 20, f32=True))
+    assert [(q["len"], q["b"]) for q in p] == [(1024, 4), (1024, 4)]
+    t = plan1d(T, S, fw, 1000, f32=True)
+    assert fw.error == T.TOPE_ERR_INVALID_SIZE and not t.impl
