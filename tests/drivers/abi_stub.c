@@ -16,6 +16,35 @@
 
 static uintptr_t g_next = 0x100000;
 
+/* call log for the tests: kind 1 = pass launch {n0, n1, n2, in, out, len or
+ * -log2 L}, kind 2 = device-to-host copy {dst, src, bytes}, kind 3 = 2D
+ * device-to-host copy {dst, src, width, height, pitch} */
+#define LOG_MAX 4096
+static int64_t g_log[LOG_MAX][8];
+static int g_nlog = 0;
+
+static void log_rec(int64_t kind, int64_t a, int64_t b, int64_t c, int64_t d, int64_t e,
+                    int64_t f)
+{
+    if (g_nlog >= LOG_MAX) return;
+    int64_t *r = g_log[g_nlog++];
+    r[0] = kind;
+    r[1] = a;
+    r[2] = b;
+    r[3] = c;
+    r[4] = d;
+    r[5] = e;
+    r[6] = f;
+    r[7] = 0;
+}
+
+void stub_log_clear(void) { g_nlog = 0; }
+int stub_log_count(void) { return g_nlog; }
+void stub_log_get(int i, int64_t *rec)
+{
+    for (int k = 0; k < 8; k++) rec[k] = (i >= 0 && i < g_nlog) ? g_log[i][k] : 0;
+}
+
 static void *token(void)
 {
     g_next += 0x1000;
@@ -31,10 +60,19 @@ int tfft_host_alloc(void **p, size_t bytes) { *p = malloc(bytes ? bytes : 16); r
 int tfft_host_free(void *p) { free(p); return 0; }
 int tfft_memset_async(void *p, int v, size_t b, void *s) { (void)p; (void)v; (void)b; (void)s; return 0; }
 int tfft_h2d(void *d, const void *s, size_t b, void *st) { (void)d; (void)s; (void)b; (void)st; return 0; }
-int tfft_d2h(void *d, const void *s, size_t b, void *st) { (void)s; (void)st; memset(d, 0, b); return 0; }
+int tfft_d2h(void *d, const void *s, size_t b, void *st)
+{
+    (void)st;
+    /* small reads are status words (the batch kernel's flags): zeros */
+    if (b <= 64) memset(d, 0, b);
+    log_rec(2, (int64_t)(uintptr_t)d, (int64_t)(uintptr_t)s, (int64_t)b, 0, 0, 0);
+    return 0;
+}
 int tfft_d2h_2d(void *d, size_t dp, const void *s, size_t sp, size_t w, size_t h, void *st)
 {
-    (void)d; (void)dp; (void)s; (void)sp; (void)w; (void)h; (void)st;
+    (void)st;
+    log_rec(3, (int64_t)(uintptr_t)d, (int64_t)(uintptr_t)s, (int64_t)w, (int64_t)h,
+            (int64_t)dp, (int64_t)sp);
     return 0;
 }
 int tfft_d2d(void *d, const void *s, size_t b, void *st) { (void)d; (void)s; (void)b; (void)st; return 0; }
@@ -68,7 +106,13 @@ int tfft_tc_b_tile(int log_l)
 }
 int tfft_tc_error(int *flag, void *s) { (void)s; *flag = 0; return 0; }
 
-int tfft_launch_pass(const tfft_pass *p, void *s) { (void)p; (void)s; return 0; }
+int tfft_launch_pass(const tfft_pass *p, void *s)
+{
+    (void)s;
+    log_rec(1, p->n[0], p->n[1], p->n[2], (int64_t)(uintptr_t)p->in, (int64_t)(uintptr_t)p->out,
+            p->len ? p->len : -(int64_t)p->log_l);
+    return 0;
+}
 
 static int log2_exact(int v)
 {

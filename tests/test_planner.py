@@ -143,3 +143,69 @@ def test_split_precision_shapes(T, S, fw):
     assert [(q["len"], q["b"]) for q in p] == [(1024, 4), (1024, 4)]
     t = plan1d(T, S, fw, 1000, f32=True)
     assert fw.error == T.TOPE_ERR_INVALID_SIZE and not t.impl
+
+
+# ---------------------------------------------------------------- read-back slicing
+def call_log(S):
+    S.stub_log_count.restype = C.c_int
+    S.stub_log_get.argtypes = [C.c_int, C.POINTER(C.c_int64)]
+    rec = (C.c_int64 * 8)()
+    out = []
+    for i in range(S.stub_log_count()):
+        S.stub_log_get(i, rec)
+        out.append(list(rec))
+    return out
+
+
+def exec_log(T, S, f, t, exec_fn, host):
+    S.stub_log_clear()
+    exec_fn(C.byref(f), C.byref(t), host.ctypes.data_as(C.POINTER(C.c_double)), T.FORWARD)
+    assert f.error == T.TOPE_SUCCESS
+    return call_log(S), host.ctypes.data
+
+
+def test_readback_slices_1d_four_step(T, S, fw):
+    """2^24 points = 4096 x 4096: pass B runs as 8 launches of 512 lines, each
+    followed by a 2D copy of 4096 rows of 512 elements (8 KB), 64 KB apart."""
+    n = 1 << 24
+    t = plan1d(T, S, fw, n)
+    log, base = exec_log(T, S, fw, t, S.tope1DExec, np.zeros(2))
+    launches = [r for r in log if r[0] == 1]
+    copies = [r for r in log if r[0] == 3]
+    assert len(launches) == 1 + 8 and not [r for r in log if r[0] == 2]
+    assert [r[1] for r in launches[1:]] == [512] * 8
+    out = launches[1][5]
+    for k, r in enumerate(copies):
+        assert r[1] - base == 16 * 512 * k and r[2] - out == 16 * 512 * k
+        assert r[3:7] == [16 * 512, 4096, 16 * 4096, 16 * 4096]
+    assert [r[5] - launches[1][5] for r in launches[1:]] == [16 * 512 * k for k in range(8)]
+
+
+def test_readback_slices_batched_rows(T, S, fw):
+    """256 rows of 2^16: the last pass is cut along the rows, 32 rows (32 MB)
+    per contiguous copy."""
+    t = plan1d(T, S, fw, 1 << 16, batch=256)
+    log, base = exec_log(T, S, fw, t, S.tope1DExec, np.zeros(2))
+    copies = [r for r in log if r[0] == 2]
+    assert len(copies) == 8
+    assert [r[1] - base for r in copies] == [k * 32 * 16 * 65536 for k in range(8)]
+    assert all(r[3] == 32 * 16 * 65536 for r in copies)
+
+
+def test_readback_slices_3d_z_pass(T, S, fw):
+    """256^3: the z pass is cut along its 65536 (x, y) lines, 8192 per slice;
+    each slice is 256 rows of 8192 elements, one per z, 1 MB apart."""
+    t = T.TopePlan3D()
+    S.tope3DPlanInit(C.byref(fw), C.byref(t), 256, 256, 256, T.C2C, None)
+    log, base = exec_log(T, S, fw, t, S.tope3DExec, np.zeros(2))
+    copies = [r for r in log if r[0] == 3]
+    assert len(copies) == 8
+    for k, r in enumerate(copies):
+        assert r[1] - base == 16 * 8192 * k
+        assert r[3:7] == [16 * 8192, 256, 16 * 65536, 16 * 65536]
+
+
+def test_readback_not_sliced_when_small_or_real(T, S, fw):
+    for t in (plan1d(T, S, fw, 1 << 20), plan1d(T, S, fw, 1 << 22, real=True)):
+        log, _ = exec_log(T, S, fw, t, S.tope1DExec, np.zeros(2))
+        assert len([r for r in log if r[0] == 2]) == 1 and not [r for r in log if r[0] == 3]
