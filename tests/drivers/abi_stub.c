@@ -17,14 +17,14 @@
 static uintptr_t g_next = 0x100000;
 
 /* call log for the tests: kind 1 = pass launch {n0, n1, n2, in, out, len or
- * -log2 L}, kind 2 = device-to-host copy {dst, src, bytes}, kind 3 = 2D
+ * -log2 L, flags: 1 conj_in, 2 conj_out, 4 scaled}, kind 2 = device-to-host copy {dst, src, bytes}, kind 3 = 2D
  * device-to-host copy {dst, src, width, height, pitch} */
 #define LOG_MAX 4096
 static int64_t g_log[LOG_MAX][8];
 static int g_nlog = 0;
 
 static void log_rec(int64_t kind, int64_t a, int64_t b, int64_t c, int64_t d, int64_t e,
-                    int64_t f)
+                    int64_t f, int64_t g)
 {
     if (g_nlog >= LOG_MAX) return;
     int64_t *r = g_log[g_nlog++];
@@ -35,7 +35,7 @@ static void log_rec(int64_t kind, int64_t a, int64_t b, int64_t c, int64_t d, in
     r[4] = d;
     r[5] = e;
     r[6] = f;
-    r[7] = 0;
+    r[7] = g;
 }
 
 void stub_log_clear(void) { g_nlog = 0; }
@@ -65,14 +65,14 @@ int tfft_d2h(void *d, const void *s, size_t b, void *st)
     (void)st;
     /* small reads are status words (the batch kernel's flags): zeros */
     if (b <= 64) memset(d, 0, b);
-    log_rec(2, (int64_t)(uintptr_t)d, (int64_t)(uintptr_t)s, (int64_t)b, 0, 0, 0);
+    log_rec(2, (int64_t)(uintptr_t)d, (int64_t)(uintptr_t)s, (int64_t)b, 0, 0, 0, 0);
     return 0;
 }
 int tfft_d2h_2d(void *d, size_t dp, const void *s, size_t sp, size_t w, size_t h, void *st)
 {
     (void)st;
     log_rec(3, (int64_t)(uintptr_t)d, (int64_t)(uintptr_t)s, (int64_t)w, (int64_t)h,
-            (int64_t)dp, (int64_t)sp);
+            (int64_t)dp, (int64_t)sp, 0);
     return 0;
 }
 int tfft_d2d(void *d, const void *s, size_t b, void *st) { (void)d; (void)s; (void)b; (void)st; return 0; }
@@ -110,7 +110,8 @@ int tfft_launch_pass(const tfft_pass *p, void *s)
 {
     (void)s;
     log_rec(1, p->n[0], p->n[1], p->n[2], (int64_t)(uintptr_t)p->in, (int64_t)(uintptr_t)p->out,
-            p->len ? p->len : -(int64_t)p->log_l);
+            p->len ? p->len : -(int64_t)p->log_l,
+            (p->conj_in ? 1 : 0) | (p->conj_out ? 2 : 0) | (p->scale != 1.0 ? 4 : 0));
     return 0;
 }
 

@@ -209,3 +209,22 @@ def test_readback_not_sliced_when_small_or_real(T, S, fw):
     for t in (plan1d(T, S, fw, 1 << 20), plan1d(T, S, fw, 1 << 22, real=True)):
         log, _ = exec_log(T, S, fw, t, S.tope1DExec, np.zeros(2))
         assert len([r for r in log if r[0] == 2]) == 1 and not [r for r in log if r[0] == 3]
+
+
+@pytest.mark.parametrize("n,batch", [(1 << 24, 1), (1 << 16, 256), (1 << 27, 1), (10 ** 6, 1)])
+def test_inverse_flags_on_first_and_last_pass(T, S, fw, n, batch):
+    """An inverse runs as conj(F(conj x)) / N: the first launch conjugates on
+    load, every launch of the last pass (each read-back slice) conjugates and
+    scales on store, and nothing in between does."""
+    t = plan1d(T, S, fw, n, batch=batch)
+    S.stub_log_clear()
+    S.tope1DExec(C.byref(fw), C.byref(t), np.zeros(2).ctypes.data_as(C.POINTER(C.c_double)),
+                 T.INVERSE)
+    assert fw.error == T.TOPE_SUCCESS
+    launches = [r for r in call_log(S) if r[0] == 1]
+    npass = len(passes(S, fw, t))
+    flags = [r[7] for r in launches]
+    assert flags[0] & 1 and not any(f & 1 for f in flags[1:])
+    last = len(launches) - (npass - 1)  # launches of the last pass
+    assert all(f & 6 == 6 for f in flags[-last:])
+    assert not any(f & 6 for f in flags[:-last])
