@@ -228,3 +228,17 @@ def test_inverse_flags_on_first_and_last_pass(T, S, fw, n, batch):
     last = len(launches) - (npass - 1)  # launches of the last pass
     assert all(f & 6 == 6 for f in flags[-last:])
     assert not any(f & 6 for f in flags[:-last])
+
+
+@pytest.mark.parametrize("dir_,flags", [(1, [0, 0, 1, 6]), (0, [0, 0, 1, 6])])
+def test_bluestein_runs_the_convolution_both_ways(T, S, fw, dir_, flags):
+    """N = 10007: each Exec runs the 32768-point sub-plan forward (plain) and
+    inverse (conjugated in and out, scaled by 1/M), whatever the direction;
+    the direction only conjugates the chirp steps around it."""
+    t = plan1d(T, S, fw, 10007)
+    S.stub_log_clear()
+    S.tope1DExec(C.byref(fw), C.byref(t), np.zeros(2).ctypes.data_as(C.POINTER(C.c_double)),
+                 dir_)
+    assert fw.error == T.TOPE_SUCCESS
+    launches = [r for r in call_log(S) if r[0] == 1]
+    assert [r[7] for r in launches] == flags
