@@ -408,7 +408,8 @@ def test_many_plans_one_framework(T, fw, orc):
 
 
 @pytest.mark.parametrize("args", [["4096"], ["1048576"], ["64", "64"], ["4", "4096"],
-                                  ["32", "32", "32"], ["4", "8", "2048"]])
+                                  ["32", "32", "32"], ["4", "8", "2048"],
+                                  ["1000"], ["100", "60"], ["30", "20", "50"]])
 def test_reference_style_c_driver(T, tmp_path, args):
     import subprocess
     from conftest import ROOT
