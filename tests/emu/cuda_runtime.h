@@ -11,6 +11,7 @@
 #include <cmath>
 #include <cstddef>
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
 #define __device__
 #define __host__
@@ -62,7 +63,73 @@ using std::min;
 inline long long min(long long a, long long b) { return a < b ? a : b; }
 typedef int cudaError_t;
 typedef void *cudaStream_t;
+typedef void *cudaEvent_t;
 enum { cudaSuccess = 0, cudaErrorInvalidValue = 1, cudaFuncAttributeMaxDynamicSharedMemorySize = 8 };
 template <class F> inline int cudaFuncSetAttribute(F, int, int) { return 0; }
 inline int cudaGetDevice(int *d) { *d = 0; return 0; }
 inline int cudaGetLastError() { return 0; }
+
+// ---- the runtime calls of the auxiliary kernels' file (fft_aux.cu), on host
+// memory: allocations are malloc, copies memcpy, streams and events tokens,
+// and a launch runs every thread of the grid in turn (those kernels use
+// neither shared memory nor barriers).
+struct dim3 {
+    unsigned x, y, z;
+    dim3(unsigned a = 1, unsigned b = 1, unsigned c = 1) : x(a), y(b), z(c) {}
+};
+extern dim3 blockDim, gridDim;
+enum cudaMemcpyKind { cudaMemcpyHostToDevice, cudaMemcpyDeviceToHost, cudaMemcpyDeviceToDevice };
+enum { cudaStreamNonBlocking = 1 };
+inline int cudaSetDevice(int) { return 0; }
+inline int cudaGetDeviceCount(int *n) { *n = 1; return 0; }
+inline int cudaMalloc(void **p, size_t b) { *p = std::calloc(1, b); return *p ? 0 : 2; }
+inline int cudaFree(void *p) { std::free(p); return 0; }
+inline int cudaMallocHost(void **p, size_t b) { return cudaMalloc(p, b); }
+inline int cudaFreeHost(void *p) { return cudaFree(p); }
+inline int cudaMemsetAsync(void *p, int v, size_t b, cudaStream_t) { std::memset(p, v, b); return 0; }
+inline int cudaMemcpyAsync(void *d, const void *s, size_t b, cudaMemcpyKind, cudaStream_t)
+{
+    std::memmove(d, s, b);
+    return 0;
+}
+inline int cudaMemcpy2DAsync(void *d, size_t dp, const void *s, size_t sp, size_t w, size_t h,
+                             cudaMemcpyKind, cudaStream_t)
+{
+    for (size_t r = 0; r < h; r++) std::memmove((char *)d + r * dp, (const char *)s + r * sp, w);
+    return 0;
+}
+inline int cudaStreamCreateWithFlags(cudaStream_t *s, int) { *s = (void *)1; return 0; }
+inline int cudaStreamDestroy(cudaStream_t) { return 0; }
+inline int cudaStreamSynchronize(cudaStream_t) { return 0; }
+inline int cudaStreamWaitEvent(cudaStream_t, cudaEvent_t, int) { return 0; }
+inline int cudaEventCreate(cudaEvent_t *e) { *e = (void *)1; return 0; }
+inline int cudaEventDestroy(cudaEvent_t) { return 0; }
+inline int cudaEventRecord(cudaEvent_t, cudaStream_t) { return 0; }
+inline int cudaEventElapsedTime(float *ms, cudaEvent_t, cudaEvent_t) { *ms = 0; return 0; }
+inline const char *cudaGetErrorString(int) { return "host stand-in"; }
+template <class F> inline void emu_launch(dim3 g, dim3 b, F f)
+{
+    gridDim = g;
+    blockDim = b;
+    for (unsigned by = 0; by < g.y; by++)
+        for (unsigned bx = 0; bx < g.x; bx++)
+            for (unsigned tx = 0; tx < b.x; tx++) {
+                blockIdx = {bx, by, 0};
+                threadIdx = {tx, 0, 0};
+                f();
+            }
+}
+// device math the auxiliary kernels call, written from the definitions
+inline void sincospi(double x, double *s, double *c)
+{
+    const long double a = (long double)x * 3.141592653589793238462643383279502884L;
+    *s = (double)sinl(a);
+    *c = (double)cosl(a);
+}
+inline float __double2float_rn(double x) { return (float)x; }
+inline unsigned __brev(unsigned v)
+{
+    unsigned r = 0;
+    for (int i = 0; i < 32; i++) r |= ((v >> i) & 1u) << (31 - i);
+    return r;
+}

@@ -9,7 +9,15 @@ for every arithmetic, with row and strided layouts, two-level and whole
 four-step tables, inverse conjugation and scale, and double-float tiles that
 take the 2^600 lift, and compares with a long-double DFT of the same lines.
 This checks the kernels' index arithmetic and butterflies without a GPU; the
-GPU tests check the compiled device code."""
+GPU tests check the compiled device code.
+
+The auxiliary kernels' file (fft_aux.cu: twiddle and four-step tables,
+real-data steps, Bluestein pieces, the exact-index DFT) runs the same way,
+its launches rewritten as a loop over the grid's threads (those kernels use
+neither shared memory nor barriers) and its runtime calls on host memory,
+through the library's own tfft_* entry points (tests/emu/aux_driver.cpp);
+sincospi is a long-double stand-in, so these cases check the angle
+reductions and indexing, not the device's sincospi."""
 import re
 import subprocess
 
@@ -21,6 +29,50 @@ CSRC = ROOT / "tope-fft_gb300" / "csrc"
 EMU = ROOT / "tests" / "emu"
 HEADERS = ["fft_pass.cuh", "fft_mixed.cuh", "fft_arith.cuh", "tfft_abi.h", "fft_mixed_consts.inc"]
 NCASES = 12
+NAUX = 7
+
+
+def split_top(s):
+    """Split a launch configuration at its top-level commas."""
+    parts, depth, cur = [], 0, ""
+    for ch in s:
+        depth += ch in "(["
+        depth -= ch in ")]"
+        if ch == "," and depth == 0:
+            parts.append(cur.strip())
+            cur = ""
+        else:
+            cur += ch
+    parts.append(cur.strip())
+    return parts
+
+
+def host_launches(src):
+    """name<<<grid, block, ...>>>(args) -> emu_launch(dim3(grid), dim3(block), ...)"""
+    out, i = [], 0
+    while True:
+        j = src.find("<<<", i)
+        if j < 0:
+            out.append(src[i:])
+            return "".join(out)
+        k = j
+        while k > 0 and (src[k - 1].isalnum() or src[k - 1] == "_"):
+            k -= 1
+        e = src.find(">>>", j)
+        cfg = split_top(src[j + 3:e])
+        a0 = e + 3
+        while src[a0].isspace():
+            a0 += 1
+        depth, a = 0, a0
+        while True:
+            depth += src[a] == "("
+            depth -= src[a] == ")"
+            if depth == 0:
+                break
+            a += 1
+        out.append(src[i:k])
+        out.append(f"emu_launch(dim3({cfg[0]}), dim3({cfg[1]}), [&] {{ {src[k:j]}({src[a0 + 1:a]}); }})")
+        i = a + 1
 
 
 @pytest.fixture(scope="module")
@@ -47,3 +99,25 @@ def test_kernel_on_cpu(emu, case):
     assert m, r.stdout
     rel, tol = float(m.group(1)), float(m.group(2))
     assert rel <= tol, r.stdout
+
+
+@pytest.fixture(scope="module")
+def aux(tmp_path_factory):
+    d = tmp_path_factory.mktemp("aux")
+    for h in ("fft_arith.cuh", "tfft_abi.h"):
+        (d / h).write_text((CSRC / h).read_text())
+    (d / "fft_aux.cpp").write_text(host_launches((CSRC / "fft_aux.cu").read_text()))
+    exe = d / "aux"
+    subprocess.run(["g++", "-std=c++20", "-O1", "-pthread", f"-I{EMU}", f"-I{d}",
+                    str(d / "fft_aux.cpp"), str(EMU / "aux_driver.cpp"), "-o", str(exe)],
+                   check=True)
+    return exe
+
+
+@pytest.mark.parametrize("case", range(NAUX))
+def test_aux_kernel_on_cpu(aux, case):
+    r = subprocess.run([str(aux), str(case)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    m = re.search(r"err=(\S+) tol=(\S+)", r.stdout)
+    assert m, r.stdout
+    assert float(m.group(1)) <= float(m.group(2)), r.stdout
