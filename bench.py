@@ -184,6 +184,12 @@ def pass_points(wl: dict) -> int:
     return n * wl["batch"]
 
 
+def sig(v: float, digits: int = 5) -> float:
+    """v to `digits` significant digits (CPU rates of the O(N^2) reference
+    path are far below 1e-4 GFLOP/s)."""
+    return float(f"{v:.{digits}g}")
+
+
 def smooth(n: int, primes) -> bool:
     for p in primes:
         while n % p == 0:
@@ -368,7 +374,7 @@ def cpu_reference_rate(wl: dict, budget_s: float = 30.0, steps: int = 1, warmup:
     gflops = flops / t / 1e9
     sample = (f"{'x'.join(map(str, sample_dims))} x batch {sample_batch}, forward+inverse, "
               f"{len(times)} timed step(s), median {t:.3f} s, {cores} threads")
-    return gflops, {"value": round(gflops, 4), "unit": "GFLOP/s", "cores": cores, "kind": kind,
+    return gflops, {"value": sig(gflops), "unit": "GFLOP/s", "cores": cores, "kind": kind,
                     "sample": sample, "ms_per_step": t * 1e3}
 
 
@@ -763,7 +769,7 @@ def run_reference(args, wl: dict):
         gflops, cpu = cpu_reference_rate(
             wl, budget_s=150.0 / max(1, args.steps + args.warmup) * args.steps,
             steps=args.steps, warmup=min(args.warmup, 1))
-    return {"impl": "reference", "metric": METRIC, "value": round(gflops, 4), "unit": "GFLOP/s",
+    return {"impl": "reference", "metric": METRIC, "value": sig(gflops), "unit": "GFLOP/s",
             "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(cpu["ms_per_step"], 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64",
@@ -771,7 +777,7 @@ def run_reference(args, wl: dict):
             "config": {"workload": args.workload, "description": wl["desc"],
                        "parallelism": "host cores of rank 0"},
             "cpu_baseline": cpu,
-            "e2e": {"value": round(gflops, 4), "unit": "GFLOP/s", "h2d_bytes_per_step": 0,
+            "e2e": {"value": sig(gflops), "unit": "GFLOP/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
 
 
