@@ -334,7 +334,7 @@ def cpu_reference_rate(wl: dict, budget_s: float = 30.0, steps: int = 1, warmup:
         gflops = flops_per_step(wl) / t / 1e9
         sample = (f"the reference DFT (O(n^2)) at n={n_s}, forward, {t_s:.3f} s on {cores} threads, "
                   f"scaled by (n/{n_s})^2 to n={n_all} and doubled for the inverse")
-        return gflops, {"value": round(gflops, 6), "unit": "GFLOP/s", "cores": cores,
+        return gflops, {"value": sig(gflops), "unit": "GFLOP/s", "cores": cores,
                         "kind": kind, "sample": sample, "ms_per_step": t * 1e3}
     if wl.get("real"):
         # the reference has no real-data path: its complex transform of the
