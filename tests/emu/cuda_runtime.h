@@ -13,6 +13,8 @@
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
+#include <thread>
+#include <vector>
 #define __device__
 #define __host__
 #define __global__
@@ -118,6 +120,31 @@ template <class F> inline void emu_launch(dim3 g, dim3 b, F f)
                 threadIdx = {tx, 0, 0};
                 f();
             }
+}
+// a launch of a kernel that synchronises its CTA: each CTA in turn, all of
+// its threads at once (one std::thread each), with the CTA and warp barriers
+template <class F> inline void emu_cta_launch(dim3 g, dim3 b, F f)
+{
+    gridDim = g;
+    blockDim = b;
+    const int threads = (int)b.x;
+    for (unsigned bx = 0; bx < g.x; bx++) {
+        blockIdx = {bx, 0, 0};
+        std::barrier<> cta(threads);
+        g_cta_bar = &cta;
+        std::barrier<> *warps[32] = {};
+        for (int w = 0; w * 32 < threads; w++)
+            g_warp_bar[w] = warps[w] = new std::barrier<>(std::min(32, threads - 32 * w));
+        std::vector<std::thread> th;
+        th.reserve(threads);
+        for (int x = 0; x < threads; x++)
+            th.emplace_back([&f, x] {
+                threadIdx = {(unsigned)x, 0, 0};
+                f();
+            });
+        for (auto &t : th) t.join();
+        for (int w = 0; w * 32 < threads; w++) delete warps[w];
+    }
 }
 // device math the auxiliary kernels call, written from the definitions
 inline void sincospi(double x, double *s, double *c)

@@ -1,0 +1,171 @@
+"""The whole library on the CPU: its C host code, the auxiliary kernels, the
+pass dispatch, and the power-of-two (log2 L <= 8, and the 4-points-per-thread
+shape), mixed-radix and real-data kernels, all built from the repository's
+own sources for the host (tests/emu/emu_build.py), each kernel launch run as
+one CTA after another with one std::thread per CUDA thread.  The tensor form,
+the persistent batch kernel and CUDA graphs are not built for the host.
+
+The tests call the public C entry points through the same ctypes mirror as
+the GPU tests and compare with the oracle: one- and multi-pass power-of-two
+lines, mixed radix, Bluestein and the exact DFT, 2D/3D, real data, both
+FP64-storage arithmetics and the split-precision modes.  Gates as on the GPU."""
+import numpy as np
+import pytest
+
+from conftest import SEED0, tol_fp64
+
+import sys
+from pathlib import Path
+sys.path.insert(0, str(Path(__file__).resolve().parent / "emu"))
+import emu_build  # noqa: E402
+
+
+@pytest.fixture(scope="module")
+def E(T, tmp_path_factory):
+    """The package's ctypes mirror, bound to the host build of the library."""
+    lib = T.load_library(emu_build.build_library(tmp_path_factory.mktemp("emulib")))
+    saved = T.topefft.lib
+    T.topefft.lib = lib
+    yield T
+    T.topefft.lib = saved
+
+
+@pytest.fixture(params=["fp64", "df64"])
+def fw(E, request):
+    f = E.TopeFFT()
+    E.topeFFTInit(f)
+    E.check(f)
+    E.topeSetArith(f, E.TOPE_ARITH_DF64 if request.param == "df64" else E.TOPE_ARITH_FP64)
+    yield f
+    E.topeFFTDestroy(f)
+
+
+def oracle_1d(orc, x, n, dir_, batch=1):
+    rows = []
+    for i in range(batch):
+        xi = x[2 * n * i: 2 * n * (i + 1)]
+        rows.append(orc.fft_ld(xi, n, dir_=dir_) if n & (n - 1) == 0 or n < 5000 else
+                    orc.bluestein_ld(xi, n, dir_))
+    return np.concatenate(rows)
+
+
+@pytest.mark.parametrize("n,batch", [(2, 1), (8, 1), (64, 1), (256, 4), (4096, 1), (1 << 14, 1),
+                                     (1000, 1), (60, 8), (1001, 1), (131, 1), (127, 2)])
+def test_1d(E, fw, orc, n, batch):
+    x = orc.uniform(n * batch, SEED0 + n)
+    for dir_ in (1, 0):
+        d = x.copy()
+        t = E.TopePlan1D()
+        E.tope1DBatchPlanInit(fw, t, n, batch, E.C2C, d)
+        E.check(fw)
+        E.tope1DExec(fw, t, d, dir_)
+        E.check(fw)
+        assert orc.rel_l2(d, oracle_1d(orc, x, n, dir_, batch)) <= tol_fp64(n)
+        E.tope1DDestroy(fw, t)
+
+
+@pytest.mark.parametrize("shape", [(32, 16, 1), (12, 10, 1), (8, 16, 4), (6, 10, 14)])
+def test_nd(E, fw, orc, shape):
+    nx, ny, nz = shape
+    x = orc.uniform(nx * ny * nz, SEED0 + nx + ny)
+    for dir_ in (1, 0):
+        d = x.copy()
+        if nz == 1:
+            t = E.TopePlan2D()
+            E.tope2DPlanInit(fw, t, nx, ny, E.C2C, d)
+            E.check(fw)
+            E.tope2DExec(fw, t, d, dir_)
+            E.tope2DDestroy(fw, t)
+        else:
+            t = E.TopePlan3D()
+            E.tope3DPlanInit(fw, t, nx, ny, nz, E.C2C, d)
+            E.check(fw)
+            E.tope3DExec(fw, t, d, dir_)
+            E.tope3DDestroy(fw, t)
+        E.check(fw)
+        assert orc.rel_l2(d, orc.fft_ld(x, nx, ny, nz, dir_=dir_)) <= tol_fp64(nx * ny * nz)
+
+
+def test_single_axes_compose(E, fw, orc):
+    """ExecX then ExecY on device data equals Exec (fft2d.c:12-133)."""
+    nx, ny = 16, 8
+    x = orc.uniform(nx * ny, SEED0 + 9)
+    t = E.TopePlan2D()
+    E.tope2DPlanInit(fw, t, nx, ny, E.C2C, x.copy())
+    E.tope2DExecX(fw, t)
+    E.tope2DExecY(fw, t)
+    got = np.empty_like(x)
+    E.download(fw, t, got)
+    E.check(fw)
+    assert orc.rel_l2(got, orc.fft_ld(x, nx, ny, 1, dir_=1)) <= tol_fp64(nx * ny)
+    E.tope2DDestroy(fw, t)
+
+
+@pytest.mark.parametrize("dims", [(64, 1, 1), (2000, 1, 1), (16, 8, 1), (20, 12, 1)])
+def test_real_data(E, fw, orc, dims):
+    nx, ny, nz = dims
+    n = nx * ny * nz
+    xr = orc.uniform(n // 2, SEED0 + nx)
+    d = np.zeros((nx + 2) * ny * nz)
+    d[:n] = xr
+    if ny == 1:
+        t = E.TopePlan1D()
+        E.tope1DPlanInit(fw, t, nx, E.R2C, d)
+        ex, ds = E.tope1DExec, E.tope1DDestroy
+    else:
+        t = E.TopePlan2D()
+        E.tope2DPlanInit(fw, t, nx, ny, E.R2C, d)
+        ex, ds = E.tope2DExec, E.tope2DDestroy
+    E.check(fw)
+    ex(fw, t, d, E.FORWARD)
+    E.check(fw)
+    z = np.zeros(2 * n)
+    z[0::2] = xr
+    full = orc.fft_ld(z, nx, ny, nz, dir_=1).reshape(nz, ny, nx, 2)
+    want = np.ascontiguousarray(full[:, :, : nx // 2 + 1, :]).ravel()
+    assert orc.rel_l2(d, want) <= tol_fp64(n)
+    ex(fw, t, d, E.INVERSE)
+    E.check(fw)
+    assert orc.rel_l2(d[:n], xr) <= tol_fp64(n)
+    ds(fw, t)
+
+
+@pytest.mark.parametrize("mode,gate", [(0, 1e-7), (1, 2.5e-7)])
+@pytest.mark.parametrize("dims,batch,real", [((256, 1, 1), 4, False), ((32, 16, 1), 1, False),
+                                             ((1000, 1, 1), 2, False), ((64, 1, 1), 3, True)])
+def test_split_precision(E, orc, mode, gate, dims, batch, real):
+    f = E.TopeFFT()
+    E.topeFFTInit(f)
+    E.topeSetSplitMode(f, mode)
+    nx, ny, nz = dims
+    n = nx * ny * nz
+    if real:
+        xr = orc.uniform(n * batch // 2, SEED0 + 3)
+        d = np.zeros((nx + 2) * batch, dtype=np.float32)
+        d[:n * batch] = xr
+    else:
+        x = orc.uniform(n * batch, SEED0 + 3)
+        d = x.astype(np.float32)
+    if ny == 1:
+        t = E.TopePlan1D()
+        E.tope1DBatchPlanInitF32(f, t, nx, batch, E.R2C if real else E.C2C, d)
+    else:
+        t = E.TopePlan2D()
+        E.tope2DPlanInitF32(f, t, nx, ny, E.C2C, d)
+    E.check(f)
+    E.execF32(f, t, d, E.FORWARD)
+    E.check(f)
+    if real:
+        want = []
+        for b in range(batch):
+            z = np.zeros(2 * nx)
+            z[0::2] = xr[b * nx:(b + 1) * nx]
+            want.append(orc.fft_ld(z, nx, dir_=1)[: nx + 2])
+        want = np.concatenate(want)
+    elif ny == 1:
+        want = oracle_1d(orc, x, nx, 1, batch)
+    else:
+        want = orc.fft_ld(x, nx, ny, nz, dir_=1)
+    assert orc.rel_l2(d.astype(np.float64), want) <= gate
+    {E.TopePlan1D: E.tope1DDestroy, E.TopePlan2D: E.tope2DDestroy}[type(t)](f, t)
+    E.topeFFTDestroy(f)
