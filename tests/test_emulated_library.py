@@ -169,3 +169,39 @@ def test_split_precision(E, orc, mode, gate, dims, batch, real):
     assert orc.rel_l2(d.astype(np.float64), want) <= gate
     {E.TopePlan1D: E.tope1DDestroy, E.TopePlan2D: E.tope2DDestroy}[type(t)](f, t)
     E.topeFFTDestroy(f)
+
+
+@pytest.mark.parametrize("shape", [(2, 2, 1), (2, 4, 8), (1, 16, 2), (4, 1, 2)])
+def test_short_axes(E, fw, orc, shape):
+    """Axes of length 1 and 2 (the reference divides by n/4 == 0 there,
+    src/kernels2D.cl:51)."""
+    nx, ny, nz = shape
+    x = orc.uniform(nx * ny * nz, SEED0 + 17)
+    d = x.copy()
+    t = E.TopePlan3D()
+    E.tope3DPlanInit(fw, t, nx, ny, nz, E.C2C, d)
+    E.check(fw)
+    E.tope3DExec(fw, t, d, E.FORWARD)
+    E.check(fw)
+    assert orc.rel_l2(d, orc.fft_ld(x, nx, ny, nz, dir_=1)) <= tol_fp64(nx * ny * nz)
+    E.tope3DDestroy(fw, t)
+
+
+@pytest.mark.parametrize("scale", [1e300, 1e-300, 2.0 ** -1060])
+def test_extreme_magnitudes(E, fw, orc, scale):
+    """Inputs near the top and bottom of the FP64 range, subnormals included.
+    The double-float arithmetic's tile scaling keeps its (hi, lo) pairs in
+    FP32 range; at 2^-1060 the inputs and outputs are FP64 subnormals with
+    about 14 significant bits, which bounds either path's accuracy (native
+    FP64 rounds every intermediate to that spacing)."""
+    n = 256
+    x = orc.uniform(n, SEED0 + 5) * scale
+    d = x.copy()
+    t = E.TopePlan1D()
+    E.tope1DPlanInit(fw, t, n, E.C2C, d)
+    E.tope1DExec(fw, t, d, E.FORWARD)
+    E.check(fw)
+    want = orc.fft_ld(x, n, dir_=1)
+    tol = tol_fp64(n) if scale >= 1e-300 else (1e-6 if fw.arith else 1e-4)
+    assert orc.rel_l2(d, want) <= tol
+    E.tope1DDestroy(fw, t)
