@@ -22,7 +22,8 @@ enum topeStatus {
     TOPE_ERR_CUDA = 4,           /* a CUDA call failed; see topeLastCudaError() */
     TOPE_ERR_NOT_INITIALIZED = 5,/* framework not initialised */
     TOPE_ERR_DESTROYED = 6,      /* plan already destroyed (double destroy, use after destroy) */
-    TOPE_ERR_UNSUPPORTED = 7,    /* valid request this build cannot run (e.g. 2D R2C) */
+    TOPE_ERR_UNSUPPORTED = 7,    /* valid request this build cannot run (e.g. the tensor
+                                    form for an uneven batch) */
     TOPE_ERR_TIMEOUT = 8         /* a bounded device-side wait expired */
 };
 
