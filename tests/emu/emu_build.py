@@ -15,6 +15,15 @@ INCLUDE = ROOT / "include"
 EMU = Path(__file__).resolve().parent
 
 
+def host_cxx_ok(tmp: Path) -> bool:
+    """Can the host C++ compiler build the stand-in (C++20 <barrier>)?"""
+    src = tmp / "probe.cpp"
+    src.write_text("#include <barrier>\nint main() { std::barrier<> b(1); b.arrive_and_wait(); }\n")
+    r = subprocess.run(["g++", "-std=c++20", "-pthread", str(src), "-o", str(tmp / "probe")],
+                       capture_output=True, text=True)
+    return r.returncode == 0
+
+
 def split_top(s: str) -> list[str]:
     """Split a launch configuration at its top-level commas (brackets and
     template angle brackets nest; << and >> are shifts)."""

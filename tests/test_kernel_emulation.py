@@ -75,9 +75,18 @@ def host_launches(src):
         i = a + 1
 
 
+def cxx20_ok(d):
+    src = d / "probe.cpp"
+    src.write_text("#include <barrier>\nint main() { std::barrier<> b(1); b.arrive_and_wait(); }\n")
+    return subprocess.run(["g++", "-std=c++20", "-pthread", str(src), "-o", str(d / "probe")],
+                          capture_output=True).returncode == 0
+
+
 @pytest.fixture(scope="module")
 def emu(tmp_path_factory):
     d = tmp_path_factory.mktemp("emu")
+    if not cxx20_ok(d):
+        pytest.skip("no C++20 host compiler (std::barrier)")
     for h in HEADERS:
         src = (CSRC / h).read_text()
         # dynamic shared memory is the stand-in's static buffer; the launch
@@ -104,6 +113,8 @@ def test_kernel_on_cpu(emu, case):
 @pytest.fixture(scope="module")
 def aux(tmp_path_factory):
     d = tmp_path_factory.mktemp("aux")
+    if not cxx20_ok(d):
+        pytest.skip("no C++20 host compiler (std::barrier)")
     for h in ("fft_arith.cuh", "tfft_abi.h"):
         (d / h).write_text((CSRC / h).read_text())
     (d / "fft_aux.cpp").write_text(host_launches((CSRC / "fft_aux.cu").read_text()))
