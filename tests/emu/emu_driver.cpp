@@ -31,6 +31,24 @@ static CLD wpow(long long m, long long n)
     return CLD(cosl(a), sinl(a));
 }
 
+#if defined(__SANITIZE_ADDRESS__)
+#include <sanitizer/asan_interface.h>
+#endif
+
+/* bytes of dynamic shared memory the current launch asked for: under
+ * AddressSanitizer the rest of the buffer is poisoned, so an access past the
+ * launch's allocation is reported */
+static size_t g_smem_bytes = sizeof(tfft::smem_raw);
+
+static void smem_limit(size_t bytes)
+{
+    g_smem_bytes = bytes;
+#if defined(__SANITIZE_ADDRESS__)
+    __asan_unpoison_memory_region(tfft::smem_raw, sizeof(tfft::smem_raw));
+    __asan_poison_memory_region(tfft::smem_raw + bytes, sizeof(tfft::smem_raw) - bytes);
+#endif
+}
+
 /* one CTA at a time, all of its threads at once */
 template <class K>
 static void run_grid(K kernel, const tfft_pass &p, long long blocks, int threads)
@@ -161,6 +179,7 @@ static void mixed(int id, const Spec &s, double tol)
         p.len = (int)s.L;
         p.nrad = nr;
         std::memcpy(p.radix, rad, nr);
+        smem_limit(tfft::mixed_smem_bytes((int)(s.L * s.B), (int)sizeof(typename A::S)));
         run_grid(tfft::mixed_kernel<A>, p, (s.lines + s.B - 1) / s.B, tfft::kMixedThreads);
     });
     std::printf("case %d mixed_kernel<%d> L=%lld B=%lld rel=%.3e tol=%.1e\n", id, A::kId, s.L, s.B,
@@ -173,6 +192,7 @@ static void pass(int id, const Spec &s, double tol)
     const double e = run_case<A>(s, [&](tfft_pass &p) {
         p.log_l = LOG_L;
         p.ept = EPT == 16 ? 0 : EPT;
+        smem_limit(tfft::pass_smem_bytes<A, LOG_L, B, EPT>());
         run_grid(tfft::pass_kernel<A, LOG_L, B, EPT>, p, (s.lines + B - 1) / B,
                  tfft::Shape<LOG_L, EPT>::TPL * B);
     });

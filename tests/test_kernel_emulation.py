@@ -100,6 +100,30 @@ def emu(tmp_path_factory):
     return exe
 
 
+@pytest.fixture(scope="module")
+def emu_san(tmp_path_factory, emu):
+    """The same driver under AddressSanitizer and UndefinedBehaviorSanitizer:
+    the part of the shared-memory buffer beyond each launch's dynamic size is
+    poisoned, so an access outside the launch's allocation is an error."""
+    d = emu.parent
+    exe = d / "emu_san"
+    r = subprocess.run(["g++", "-std=c++20", "-O1", "-g", "-pthread",
+                        "-fsanitize=address,undefined", "-fno-sanitize-recover=undefined",
+                        f"-I{d}", f"-I{EMU}", str(EMU / "emu_driver.cpp"), "-o", str(exe)],
+                       capture_output=True, text=True)
+    if r.returncode:
+        pytest.skip("no sanitizer runtime for the host compiler")
+    return exe
+
+
+@pytest.mark.parametrize("case", range(NCASES))
+def test_kernel_under_sanitizers(emu_san, case):
+    r = subprocess.run([str(emu_san), str(case)], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0 and "runtime error" not in r.stderr, r.stderr[-2000:]
+    m = re.search(r"rel=(\S+) tol=(\S+)", r.stdout)
+    assert m and float(m.group(1)) <= float(m.group(2)), r.stdout
+
+
 @pytest.mark.parametrize("case", range(NCASES))
 def test_kernel_on_cpu(emu, case):
     r = subprocess.run([str(emu), str(case)], capture_output=True, text=True, timeout=300)
