@@ -63,7 +63,7 @@ def main() -> None:
         x[0::2] = np.sin(2 * np.pi * np.arange(n) / n)
         g[f"sin_fwd_{nx}x{ny}x{nz}"] = ref.exec(x, nx, ny, nz, 1)
     # non-power-of-two lengths: the reference's DFT kernel (forward only)
-    for n in (3, 5, 6, 7, 12, 27, 100):
+    for n in (3, 5, 6, 7, 11, 12, 13, 27, 100, 1000, 1001):
         seed = SEED0 + 2000 + n
         x = orc.uniform(n, seed)
         g[f"dftseed_{n}"] = np.array([seed], dtype=np.uint64)

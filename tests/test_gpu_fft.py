@@ -131,7 +131,7 @@ def test_1d_two_point(T, fw, orc, golden):
     assert orc.rel_l2(run1d(T, fw, x, 2, 0), orc.fft_ld(x, 2, dir_=0)) <= 1e-16
 
 
-@pytest.mark.parametrize("n", [3, 5, 6, 7, 12, 27, 100, 1000])
+@pytest.mark.parametrize("n", [3, 5, 6, 7, 11, 12, 13, 27, 100, 1000, 1001])
 def test_1d_non_power_of_two(T, fw, orc, golden, n):
     key = f"dftseed_{n}"
     x = orc.uniform(n, int(golden[key][0]) if key in golden else SEED0 + n)

@@ -106,14 +106,16 @@ def test_reference_driver_inputs(orc, golden):
         assert orc.rel_l2(orc.exec(x, nx, ny, nz), golden[f"sin_fwd_{nx}x{ny}x{nz}"]) <= PIN_TOL
 
 
-@pytest.mark.parametrize("n", [3, 5, 6, 7, 12, 27, 100])
+@pytest.mark.parametrize("n", [3, 5, 6, 7, 11, 12, 13, 27, 100, 1000, 1001])
 def test_dft_path(orc, golden, n):
     x = orc.uniform(n, int(golden[f"dftseed_{n}"][0]))
     ref = golden[f"dft_{n}"]
     # same expression order as kernels1D.cl:561-564, so bit for bit
     assert np.array_equal(orc.dft_ref(x, n), ref)
-    # the reference's DFT is a correct forward transform
-    assert orc.rel_l2(ref, orc.dft_ld(x, n, 1)) <= 1e-13
+    # the reference's DFT is a correct forward transform, to the FP64 gate
+    # (its unreduced angle 2 pi j k / n loses accuracy as j k grows: 1.8e-13
+    # at n = 1000 against 2e-16 for an exact-index sum)
+    assert orc.rel_l2(ref, orc.dft_ld(x, n, 1)) <= 1e-13 * max(1.0, np.log2(n))
 
 
 def test_swap_pass_is_bit_reversal(orc, golden):
