@@ -208,3 +208,17 @@ def test_extreme_magnitudes(E, fw, orc, scale):
     tol = tol_fp64(n) if scale >= 1e-300 else (1e-6 if fw.arith else 1e-4)
     assert orc.rel_l2(d, want) <= tol
     E.tope1DDestroy(fw, t)
+
+
+@pytest.mark.parametrize("n", [3, 5, 6, 7, 11, 12, 13, 27, 100, 1000, 1001])
+def test_reference_dft_outputs(E, fw, orc, golden, n):
+    """The reference's own DFT kernel outputs (tests/golden), reproduced by
+    the mixed-radix passes to the FP64 gate."""
+    x = orc.uniform(n, int(golden[f"dftseed_{n}"][0]))
+    d = x.copy()
+    t = E.TopePlan1D()
+    E.tope1DPlanInit(fw, t, n, E.C2C, d)
+    E.tope1DExec(fw, t, d, E.FORWARD)
+    E.check(fw)
+    assert orc.rel_l2(d, golden[f"dft_{n}"]) <= tol_fp64(n)
+    E.tope1DDestroy(fw, t)
