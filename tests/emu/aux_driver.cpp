@@ -17,6 +17,7 @@ dim3 blockDim, gridDim;
 std::barrier<> *g_cta_bar;
 std::barrier<> *g_warp_bar[32];
 unsigned g_warp_val[32][32];
+emu_graph *g_capture;
 
 using LD = long double;
 using CLD = std::complex<LD>;

@@ -13,6 +13,7 @@
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <thread>
 #include <vector>
 #define __device__
@@ -59,6 +60,10 @@ inline unsigned atomicMax(unsigned *p, unsigned v)
     return o;
 }
 inline int __ffs(int x) { return __builtin_ffs(x); }
+inline int atomicAdd(int *p, int v) { return std::atomic_ref<int>(*p).fetch_add(v); }
+inline int atomicExch(int *p, int v) { return std::atomic_ref<int>(*p).exchange(v); }
+inline void __threadfence() { std::atomic_thread_fence(std::memory_order_seq_cst); }
+inline void __nanosleep(unsigned) { std::this_thread::yield(); }
 using std::fma;
 using std::max;
 using std::min;
@@ -88,7 +93,7 @@ inline int cudaMalloc(void **p, size_t b) { *p = std::calloc(1, b); return *p ? 
 inline int cudaFree(void *p) { std::free(p); return 0; }
 inline int cudaMallocHost(void **p, size_t b) { return cudaMalloc(p, b); }
 inline int cudaFreeHost(void *p) { return cudaFree(p); }
-inline int cudaMemsetAsync(void *p, int v, size_t b, cudaStream_t) { std::memset(p, v, b); return 0; }
+inline int cudaMemsetAsync(void *p, int v, size_t b, cudaStream_t);
 inline int cudaMemcpyAsync(void *d, const void *s, size_t b, cudaMemcpyKind, cudaStream_t)
 {
     std::memmove(d, s, b);
@@ -109,7 +114,53 @@ inline int cudaEventDestroy(cudaEvent_t) { return 0; }
 inline int cudaEventRecord(cudaEvent_t, cudaStream_t) { return 0; }
 inline int cudaEventElapsedTime(float *ms, cudaEvent_t, cudaEvent_t) { *ms = 0; return 0; }
 inline const char *cudaGetErrorString(int) { return "host stand-in"; }
-template <class F> inline void emu_launch(dim3 g, dim3 b, F f)
+// stream capture: while a capture is open, launches and memsets are recorded
+// (their arguments copied) and a launched graph replays them in order
+using emu_graph = std::vector<std::function<void()>>;
+extern emu_graph *g_capture;
+typedef emu_graph *cudaGraph_t;
+typedef emu_graph *cudaGraphExec_t;
+enum { cudaStreamCaptureModeThreadLocal = 1, cudaDevAttrMultiProcessorCount = 16 };
+inline int cudaStreamBeginCapture(cudaStream_t, int)
+{
+    if (g_capture) return 1;
+    g_capture = new emu_graph;
+    return 0;
+}
+inline int cudaStreamEndCapture(cudaStream_t, cudaGraph_t *g)
+{
+    *g = g_capture;
+    g_capture = nullptr;
+    return *g ? 0 : 1;
+}
+inline int cudaGraphInstantiate(cudaGraphExec_t *x, cudaGraph_t g, int)
+{
+    *x = new emu_graph(*g);
+    return 0;
+}
+inline int cudaMemsetAsync(void *p, int v, size_t b, cudaStream_t)
+{
+    if (g_capture) g_capture->push_back([p, v, b] { std::memset(p, v, b); });
+    else std::memset(p, v, b);
+    return 0;
+}
+inline int cudaGraphDestroy(cudaGraph_t g) { delete g; return 0; }
+inline int cudaGraphExecDestroy(cudaGraphExec_t x) { delete x; return 0; }
+inline int cudaGraphLaunch(cudaGraphExec_t x, cudaStream_t)
+{
+    for (auto &f : *x) f();
+    return 0;
+}
+// one CTA at a time: a persistent grid runs as a single CTA, which takes the
+// work items in their (topological) order
+template <class K> inline int cudaOccupancyMaxActiveBlocksPerMultiprocessor(int *n, K, int, size_t)
+{
+    *n = 1;
+    return 0;
+}
+inline int cudaDeviceGetAttribute(int *v, int, int) { *v = 1; return 0; }
+
+template <class F> inline void emu_launch_now(dim3 g, dim3 b, F f)
 {
     gridDim = g;
     blockDim = b;
@@ -123,7 +174,7 @@ template <class F> inline void emu_launch(dim3 g, dim3 b, F f)
 }
 // a launch of a kernel that synchronises its CTA: each CTA in turn, all of
 // its threads at once (one std::thread each), with the CTA and warp barriers
-template <class F> inline void emu_cta_launch(dim3 g, dim3 b, F f)
+template <class F> inline void emu_cta_launch_now(dim3 g, dim3 b, F f)
 {
     gridDim = g;
     blockDim = b;
@@ -145,6 +196,16 @@ template <class F> inline void emu_cta_launch(dim3 g, dim3 b, F f)
         for (auto &t : th) t.join();
         for (int w = 0; w * 32 < threads; w++) delete warps[w];
     }
+}
+template <class F> inline void emu_launch(dim3 g, dim3 b, F f)
+{
+    if (g_capture) g_capture->push_back([g, b, f] { emu_launch_now(g, b, f); });
+    else emu_launch_now(g, b, f);
+}
+template <class F> inline void emu_cta_launch(dim3 g, dim3 b, F f)
+{
+    if (g_capture) g_capture->push_back([g, b, f] { emu_cta_launch_now(g, b, f); });
+    else emu_cta_launch_now(g, b, f);
 }
 // device math the auxiliary kernels call, written from the definitions
 inline void sincospi(double x, double *s, double *c)

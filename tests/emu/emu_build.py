@@ -47,7 +47,8 @@ def split_top(s: str) -> list[str]:
 
 
 def host_launches(src: str, fn: str) -> str:
-    """name<<<grid, block, ...>>>(args) -> fn(dim3(grid), dim3(block), [&] { name(args); })"""
+    """name<<<grid, block, ...>>>(args) -> fn(dim3(grid), dim3(block), [=] { name(args); });
+    the arguments are copied, so a launch recorded in a graph can run later"""
     out, i = [], 0
     while True:
         j = src.find("<<<", i)
@@ -70,12 +71,17 @@ def host_launches(src: str, fn: str) -> str:
                 break
             a += 1
         out.append(src[i:k])
-        out.append(f"{fn}(dim3({cfg[0]}), dim3({cfg[1]}), [&] {{ {src[k:j]}({src[a0 + 1:a]}); }})")
+        out.append(f"{fn}(dim3({cfg[0]}), dim3({cfg[1]}), [=] {{ {src[k:j]}({src[a0 + 1:a]}); }})")
         i = a + 1
+
+
+ACQUIRE_ASM = 'asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");'
 
 
 def host_source(name: str) -> str:
     src = (CSRC / name).read_text().replace("extern __shared__", "extern")
+    # the batch kernel's acquire load, as a host atomic load
+    src = src.replace(ACQUIRE_ASM, "v = __atomic_load_n(p, __ATOMIC_ACQUIRE);")
     fn = "emu_launch" if name == "fft_aux.cu" else "emu_cta_launch"
     return host_launches(src, fn)
 
@@ -93,17 +99,19 @@ def build_library(dst: Path) -> Path:
     """The library with every kernel on the host (tests/test_emulated_library.py):
     host code (topefft.c, batch.c), the auxiliary kernels, the pass dispatch,
     the mixed-radix and 4-points-per-thread kernels, and the power-of-two pass
-    kernel for log2 L <= 8 in all four arithmetics (tests/emu/emu_launchers.cpp).
-    The tensor form, the persistent batch kernel and the allocation-free entry
-    point are left out (tests/emu/emu_rest.cpp)."""
-    prepare(dst, ["fft_arith.cuh", "fft_pass.cuh", "fft_mixed.cuh", "tfft_abi.h",
+    kernel for log2 L <= 8 in all four arithmetics (tests/emu/emu_launchers.cpp),
+    and the persistent batch kernel with its graphs (one CTA, recorded launches).
+    The tensor form and the allocation-free entry point are left out
+    (tests/emu/emu_rest.cpp)."""
+    batch = ["fft_batch_host", "fft_batch_f64", "fft_batch_df64", "fft_batch_f32", "fft_batch_df32"]
+    prepare(dst, ["fft_arith.cuh", "fft_pass.cuh", "fft_mixed.cuh", "fft_batch.cuh", "tfft_abi.h",
                   "fft_mixed_consts.inc", "topefft_internal.h", "fft_aux.cu", "fft_dispatch.cu",
-                  "fft_inst_mixed.cu", "fft_inst_small.cu"])
+                  "fft_inst_mixed.cu", "fft_inst_small.cu"] + [b + ".cu" for b in batch])
     cxx = ["g++", "-std=c++20", "-O1", "-fPIC", "-pthread", f"-I{EMU}", f"-I{dst}", f"-I{INCLUDE}"]
     cc = ["gcc", "-std=gnu11", "-O1", "-fPIC", f"-I{dst}", f"-I{INCLUDE}"]
     jobs = [cc + ["-c", str(CSRC / "topefft.c"), "-o", str(dst / "topefft.o")],
             cc + ["-c", str(CSRC / "batch.c"), "-o", str(dst / "batch.o")]]
-    for name in ["fft_aux", "fft_dispatch", "fft_inst_mixed", "fft_inst_small"]:
+    for name in ["fft_aux", "fft_dispatch", "fft_inst_mixed", "fft_inst_small"] + batch:
         jobs.append(cxx + ["-c", str(dst / f"{name}.cpp"), "-o", str(dst / f"{name}.o")])
     for arith in range(4):
         jobs.append(cxx + [f"-DEMU_ARITH={arith}", "-c", str(EMU / "emu_launchers.cpp"),

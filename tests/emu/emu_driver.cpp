@@ -18,6 +18,7 @@ uint3v blockIdx;
 std::barrier<> *g_cta_bar;
 std::barrier<> *g_warp_bar[32];
 unsigned g_warp_val[32][32];
+emu_graph *g_capture;
 namespace tfft {
 alignas(16) unsigned char smem_raw[1 << 18];
 }

@@ -222,3 +222,46 @@ def test_reference_dft_outputs(E, fw, orc, golden, n):
     E.check(fw)
     assert orc.rel_l2(d, golden[f"dft_{n}"]) <= tol_fp64(n)
     E.tope1DDestroy(fw, t)
+
+
+# ---------------------------------------------------------------- uneven batches
+# lines of at most 2^8 points per pass: the host build's launch tables stop
+# there (2^14 is two passes of 2^7)
+BATCH_SHAPES = [(64, 1), (256, 1), (16, 1), (1 << 14, 1), (64, 1), (32, 16), (8, 64), (128, 1),
+                (8, 1), (2, 1)]
+
+
+@pytest.mark.parametrize("mode", [0, 1, 2], ids=["persistent", "launch_graph", "loop"])
+@pytest.mark.parametrize("arith", ["fp64", "df64", "split"])
+def test_uneven_batch(E, orc, mode, arith, tmp_path, monkeypatch):
+    """A batch of mixed 1D/2D power-of-two transforms packed in one buffer, in
+    each execution structure: the persistent kernel (a single CTA on the host,
+    taking the work items in their topological order), the captured per-class
+    launch graph, and the per-transform loop."""
+    monkeypatch.setenv("TOPEFFT_TUNE_CACHE", str(tmp_path / "tune.txt"))
+    f = E.TopeFFT()
+    E.topeFFTInit(f)
+    if arith == "df64":
+        E.topeSetArith(f, E.TOPE_ARITH_DF64)
+    nx = [s[0] for s in BATCH_SHAPES]
+    ny = [s[1] for s in BATCH_SHAPES]
+    total = sum(a * b for a, b in BATCH_SHAPES)
+    x = orc.uniform(total, SEED0 + 77)
+    b = E.TopeBatch()
+    d = x.astype(np.float32) if arith == "split" else x.copy()
+    E.topeBatchPlanInit(f, b, nx, ny, E.C2C, d)  # FP32 data: the split-precision form
+    E.check(f)
+    assert b.classes == 9
+    E.topeBatchSetMode(f, b, mode)
+    E.check(f)
+    E.topeBatchExec(f, b, d, E.FORWARD)
+    E.check(f)
+    off = 0
+    for (a, c) in BATCH_SHAPES:
+        n = a * c
+        want = orc.fft_ld(x[2 * off: 2 * (off + n)], a, c, 1, dir_=1)
+        got = d[2 * off: 2 * (off + n)].astype(np.float64)
+        assert orc.rel_l2(got, want) <= (1e-7 if arith == "split" else tol_fp64(n)), (a, c)
+        off += n
+    E.topeBatchDestroy(f, b)
+    E.topeFFTDestroy(f)
