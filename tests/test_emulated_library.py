@@ -265,3 +265,49 @@ def test_uneven_batch(E, orc, mode, arith, tmp_path, monkeypatch):
         off += n
     E.topeBatchDestroy(f, b)
     E.topeFFTDestroy(f)
+
+
+def test_sliced_readback_rows(E, orc):
+    """Exec into a host buffer of 32 MB (256-point rows x 8192): the last pass
+    runs in slices, each copied back while the next computes; the result is
+    bit for bit that of ExecDevice + Download, and the oracle's."""
+    f = E.TopeFFT()
+    E.topeFFTInit(f)
+    nx, batch = 256, 8192
+    x = orc.uniform(nx * batch, SEED0 + 81)
+    t = E.TopePlan1D()
+    E.tope1DBatchPlanInit(f, t, nx, batch, E.C2C, x.copy())
+    E.check(f)
+    got = np.full_like(x, np.nan)
+    E.tope1DExec(f, t, got, E.FORWARD)
+    E.check(f)
+    E.upload(f, t, x)
+    E.execDevice(f, t, E.FORWARD)
+    want = np.empty_like(x)
+    E.download(f, t, want)
+    E.check(f)
+    assert np.array_equal(got, want)
+    rows = np.arange(0, batch, 911)
+    ref = np.concatenate([orc.fft_ld(x[2 * nx * r: 2 * nx * (r + 1)], nx, dir_=1) for r in rows])
+    sub = np.concatenate([got[2 * nx * r: 2 * nx * (r + 1)] for r in rows])
+    assert orc.rel_l2(sub, ref) <= tol_fp64(nx)
+    E.tope1DDestroy(f, t)
+    E.topeFFTDestroy(f)
+
+
+def test_sliced_readback_3d(E, orc):
+    """128^3 (32 MB): the z pass is sliced along its (x, y) lines and each
+    slice goes back as a 2D copy of 128 rows."""
+    f = E.TopeFFT()
+    E.topeFFTInit(f)
+    n = 128
+    x = orc.uniform(n ** 3, SEED0 + 82)
+    t = E.TopePlan3D()
+    E.tope3DPlanInit(f, t, n, n, n, E.C2C, x.copy())
+    E.check(f)
+    got = np.full_like(x, np.nan)
+    E.tope3DExec(f, t, got, E.FORWARD)
+    E.check(f)
+    assert orc.rel_l2(got, orc.fft_ld(x, n, n, n, dir_=1)) <= tol_fp64(n ** 3)
+    E.tope3DDestroy(f, t)
+    E.topeFFTDestroy(f)
