@@ -171,16 +171,21 @@ def flops_per_step(wl: dict) -> float:
 def pass_points(wl: dict) -> int:
     """Complex points one pass launch of the dominant kernel moves: the array,
     its packed half for real data, or, for a 1D length with a prime factor
-    above 13, the 2^a 3^b 5^c 7^d sub-transform of its Bluestein plan."""
+    above 13, the sub-transform of its Bluestein plan."""
     nx, ny, nz = wl["dims"]
     n = nx * ny * nz
     if wl.get("real"):
         return n // 2 * wl["batch"]
     if ny * nz == 1 and n >= 128 and not smooth(n, (2, 3, 5, 7, 11, 13)):
+        # the library's choice: the next power of two >= 2n - 1, or the
+        # smallest 2^a 3^b 5^c 7^d >= 2n - 1 when that is at most 0.6 of it
+        mp = 1
+        while mp < 2 * n - 1:
+            mp *= 2
         m = 2 * n - 1
         while not smooth(m, (2, 3, 5, 7)):
             m += 1
-        return m * wl["batch"]
+        return (m if 10 * m <= 6 * mp else mp) * wl["batch"]
     return n * wl["batch"]
 
 
