@@ -311,3 +311,69 @@ def test_sliced_readback_3d(E, orc):
     assert orc.rel_l2(got, orc.fft_ld(x, n, n, n, dir_=1)) <= tol_fp64(n ** 3)
     E.tope3DDestroy(f, t)
     E.topeFFTDestroy(f)
+
+
+def test_inverse_from_uploaded_spectrum(E, orc):
+    """2D R2C (FP64) and 1D R2C (FP32): a spectrum uploaded from the host goes
+    back to the reals through the inverse."""
+    f = E.TopeFFT()
+    E.topeFFTInit(f)
+    nx, ny = 32, 8
+    xr = orc.uniform(nx * ny // 2, SEED0 + 91)
+    z = np.zeros(2 * nx * ny)
+    z[0::2] = xr
+    spec = np.ascontiguousarray(orc.fft_ld(z, nx, ny, 1, dir_=1).reshape(ny, nx, 2)[:, : nx // 2 + 1])
+    t = E.TopePlan2D()
+    E.tope2DPlanInit(f, t, nx, ny, E.R2C, np.zeros(nx * ny))
+    E.check(f)
+    E.upload_spectrum(f, t, spec.ravel())
+    E.check(f)
+    out = np.zeros((nx + 2) * ny)
+    E.tope2DExec(f, t, out, E.INVERSE)
+    E.check(f)
+    assert orc.rel_l2(out[: nx * ny], xr) <= tol_fp64(nx * ny)
+    E.tope2DDestroy(f, t)
+    E.topeSetSplitMode(f, 0)
+    n = 128
+    zr = np.zeros(2 * n)
+    zr[0::2] = xr[:n]
+    spec1 = orc.fft_ld(zr, n, dir_=1)[: n + 2].astype(np.float32)
+    t1 = E.TopePlan1D()
+    E.tope1DBatchPlanInitF32(f, t1, n, 1, E.R2C, np.zeros(n, dtype=np.float32))
+    E.check(f)
+    E.upload_spectrum(f, t1, spec1)
+    E.check(f)
+    back = np.zeros(n + 2, dtype=np.float32)
+    E.execF32(f, t1, back, E.INVERSE)
+    E.check(f)
+    assert orc.rel_l2(back[:n].astype(np.float64), xr[:n]) <= 1e-7
+    E.tope1DDestroy(f, t1)
+    E.topeFFTDestroy(f)
+
+
+def test_status_paths(E, orc):
+    """Errors come back as statuses: a bad direction, a destroyed plan, the
+    tensor form where this build has no kernel for it, an FP64 call on an FP32
+    plan."""
+    f = E.TopeFFT()
+    E.topeFFTInit(f)
+    t = E.TopePlan1D()
+    x = orc.uniform(64, 1)
+    E.tope1DPlanInit(f, t, 64, E.C2C, x.copy())
+    E.check(f)
+    E.tope1DExec(f, t, x.copy(), 7)
+    assert f.error == E.TOPE_ERR_INVALID_ARG
+    E.tope1DDestroy(f, t)
+    E.tope1DDestroy(f, t)
+    assert f.error == E.TOPE_ERR_DESTROYED
+    E.topeSetSplitMode(f, 2)
+    t2 = E.TopePlan1D()
+    E.tope1DBatchPlanInitF32(f, t2, 256, 4, E.C2C, np.zeros(2048, dtype=np.float32))
+    assert f.error == E.TOPE_ERR_UNSUPPORTED and not t2.impl
+    E.topeSetSplitMode(f, 0)
+    E.tope1DBatchPlanInitF32(f, t2, 256, 4, E.C2C, np.zeros(2048, dtype=np.float32))
+    E.check(f)
+    E.tope1DExec(f, t2, np.zeros(2048), E.FORWARD)
+    assert f.error == E.TOPE_ERR_INVALID_ARG
+    E.tope1DDestroy(f, t2)
+    E.topeFFTDestroy(f)
