@@ -377,3 +377,84 @@ def test_status_paths(E, orc):
     assert f.error == E.TOPE_ERR_INVALID_ARG
     E.tope1DDestroy(f, t2)
     E.topeFFTDestroy(f)
+
+
+def _smooth(rng, maxn):
+    while True:
+        n = 1
+        for p in (2, 3, 5, 7, 11, 13):
+            n *= p ** int(rng.integers(0, 4 if p < 7 else 2))
+        if 2 <= n <= maxn:
+            return n
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_random_plans(E, orc, seed):
+    """Seeded random plans: 1D/2D/3D, C2C and R2C, FP64, double-float and
+    split precision, products of 2..13 and powers of two, batched rows, both
+    directions, each against the oracle.  Plans whose pass lengths the host
+    build has no kernel for (power-of-two passes above 2^8) are skipped."""
+    rng = np.random.default_rng(seed)
+    checked = 0
+    for it in range(12):
+        mode = ["fp64", "df64", "f32acc", "f32fast"][int(rng.integers(0, 4))]
+        real = bool(rng.integers(0, 3) == 0)
+        nd = int(rng.choice([1, 1, 2, 3]))
+        dir_ = int(rng.integers(0, 2))
+        nx = 2 * _smooth(rng, 150) if real else _smooth(rng, 300)
+        ny = _smooth(rng, 20) if nd >= 2 else 1
+        nz = _smooth(rng, 10) if nd == 3 else 1
+        batch = int(rng.integers(1, 4)) if nd == 1 else 1
+        if real:
+            dir_ = 1
+        f32 = mode.startswith("f32")
+        f = E.TopeFFT()
+        E.topeFFTInit(f)
+        E.topeSetArith(f, E.TOPE_ARITH_DF64 if mode == "df64" else E.TOPE_ARITH_FP64)
+        E.topeSetSplitMode(f, 1 if mode == "f32fast" else 0)
+        n = nx * ny * nz
+        if real:
+            xr = orc.uniform(n * batch // 2, seed * 100 + it)
+            d = np.zeros((nx + 2) * ny * nz * batch, dtype=np.float32 if f32 else np.float64)
+            d[: n * batch] = xr
+        else:
+            x = orc.uniform(n * batch, seed * 100 + it)
+            d = x.astype(np.float32) if f32 else x.copy()
+        kind = E.R2C if real else E.C2C
+        if nd == 1:
+            t = E.TopePlan1D()
+            (E.tope1DBatchPlanInitF32 if f32 else E.tope1DBatchPlanInit)(f, t, nx, batch, kind, d)
+        elif nd == 2:
+            t = E.TopePlan2D()
+            (E.tope2DPlanInitF32 if f32 else E.tope2DPlanInit)(f, t, nx, ny, kind, d)
+        else:
+            t = E.TopePlan3D()
+            (E.tope3DPlanInitF32 if f32 else E.tope3DPlanInit)(f, t, nx, ny, nz, kind, d)
+        if f.error == E.TOPE_ERR_UNSUPPORTED:
+            E.topeFFTDestroy(f)
+            continue
+        E.check(f)
+        if f32:
+            E.execF32(f, t, d, dir_)
+        else:
+            {E.TopePlan1D: E.tope1DExec, E.TopePlan2D: E.tope2DExec,
+             E.TopePlan3D: E.tope3DExec}[type(t)](f, t, d, dir_)
+        E.check(f)
+        if real:
+            want = []
+            for b in range(batch):
+                z = np.zeros(2 * n)
+                z[0::2] = xr[b * n:(b + 1) * n]
+                full = orc.fft_ld(z, nx, ny, nz, dir_=1).reshape(nz, ny, nx, 2)
+                want.append(np.ascontiguousarray(full[:, :, : nx // 2 + 1, :]).ravel())
+            want = np.concatenate(want)
+        else:
+            want = np.concatenate([orc.fft_ld(x[2 * n * b: 2 * n * (b + 1)], nx, ny, nz, dir_=dir_)
+                                   for b in range(batch)])
+        gate = {"f32acc": 1e-7, "f32fast": 2.5e-7}.get(mode, tol_fp64(n))
+        assert orc.rel_l2(d.astype(np.float64), want) <= gate, (mode, real, nx, ny, nz, batch)
+        {E.TopePlan1D: E.tope1DDestroy, E.TopePlan2D: E.tope2DDestroy,
+         E.TopePlan3D: E.tope3DDestroy}[type(t)](f, t)
+        E.topeFFTDestroy(f)
+        checked += 1
+    assert checked >= 6
