@@ -206,8 +206,8 @@ int main(int argc, char **argv)
     using namespace tfft;
     const int only = argc > 1 ? std::atoi(argv[1]) : -1;
     auto want = [&](int i) { return only < 0 || only == i; };
-    if (want(0)) mixed<ArithF64>(0, {400, 4, 250, true, 0, false, 1.0}, 1e-14);
-    if (want(1)) mixed<ArithF64>(1, {400, 4, 250, false, 0, false, 1.0}, 1e-14);
+    if (want(0)) mixed<ArithF64>(0, {400, 4, 30, true, 0, false, 1.0}, 1e-14);
+    if (want(1)) mixed<ArithF64>(1, {400, 4, 30, false, 0, false, 1.0}, 1e-14);
     if (want(2)) mixed<ArithF64>(2, {1000, 2, 8, false, 1, false, 1.0}, 1e-14);
     if (want(3)) mixed<ArithF64>(3, {1001, 1, 2, true, 0, true, 1.0}, 1e-14);
     if (want(4)) mixed<ArithDF64>(4, {250, 8, 16, true, 0, false, 1e-280}, 1e-13);
