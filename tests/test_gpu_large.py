@@ -102,3 +102,37 @@ def test_1d_three_passes_f32(T, mode):
     assert np.sqrt(np.sum((a - b) ** 2) / np.sum(b * b)) <= GATES[mode]
     T.tope1DDestroy(f, t)
     T.topeFFTDestroy(f)
+
+
+def test_1d_three_passes_mixed_radix(T, fw):
+    """3^16 = 43,046,721 points: more than two 4096-point passes can hold, so
+    three mixed-radix passes (split 2187 x 2187 x 9 or similar), with
+    four-step factors of a length that is not a power of two at two levels.
+    Input: two tones, whose spectrum is known exactly; then the round trip."""
+    n = 3 ** 16
+    tones = ((1234567, 1.0), (n - 5, 0.5j))
+    j = np.arange(n, dtype=np.int64)
+    z = np.zeros(n, dtype=np.complex128)
+    for k, a in tones:
+        z += a * np.exp(2j * np.pi * (((j * k) % n).astype(np.float64) / n))
+    x = z.view(np.float64).copy()
+    del z, j
+    d = x.copy()
+    t = T.TopePlan1D()
+    T.tope1DPlanInit(fw, t, n, T.C2C, d)
+    T.check(fw)
+    passes = T.pass_times(fw, t)
+    assert len(passes) == 3 and int(np.prod([p["len"] for p in passes])) == n
+    T.tope1DExec(fw, t, d, T.FORWARD)
+    T.check(fw)
+    y = d.view(np.complex128).copy()
+    ref2 = 0.0
+    for k, a in tones:
+        y[k] -= n * a
+        ref2 += abs(n * a) ** 2
+    assert np.sqrt(float(np.vdot(y, y).real) / ref2) <= 1e-13 * np.log2(n)
+    del y
+    T.tope1DExec(fw, t, d, T.INVERSE)
+    T.check(fw)
+    assert np.sqrt(np.sum((d - x) ** 2) / np.sum(x * x)) <= 1e-13 * np.log2(n)
+    T.tope1DDestroy(fw, t)
