@@ -106,7 +106,7 @@ def test_1d_three_passes_f32(T, mode):
 
 def test_1d_three_passes_mixed_radix(T, fw):
     """3^16 = 43,046,721 points: more than two 4096-point passes can hold, so
-    three mixed-radix passes (split 2187 x 2187 x 9 or similar), with
+    three mixed-radix passes (243 x 243 x 729), with
     four-step factors of a length that is not a power of two at two levels.
     Input: two tones, whose spectrum is known exactly; then the round trip."""
     n = 3 ** 16
