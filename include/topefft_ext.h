@@ -96,8 +96,8 @@ void tope1DBatchPlanInit(struct topeFFT *f, struct topePlan1D *t, int x, int bat
  * The complex work is a transform of length x/2 on the packed reals
  * (x[2j] + i x[2j+1]) plus one pre/post pass with W_x^k twiddles. */
 void tope1DUploadSpectrum(struct topeFFT *f, struct topePlan1D *t, const double *spec);
-/* tope2DPlanInit / tope3DPlanInit with type R2C (x even, y and z powers of
- * two): x*y(*z) reals in, x fastest; Exec(FORWARD) writes the (x/2 + 1)*y(*z)
+/* tope2DPlanInit / tope3DPlanInit with type R2C (x even; x/2, y and z
+ * products of 2, 3, 5, 7, 11, 13): x*y(*z) reals in, x fastest; Exec(FORWARD) writes the (x/2 + 1)*y(*z)
  * complex outputs X[kx][ky][kz], kx <= x/2, kx fastest, so d must hold
  * (x + 2)*y(*z) doubles; Exec(INVERSE) returns the reals scaled by
  * 1/(x*y*z).  The rows along x are a batched 1D real-data transform, then

@@ -12,6 +12,12 @@ SEED0 = 0x70E0F0F7
 GOLDEN = ROOT / "tests" / "golden" / "reference_golden.npz"
 
 
+def pytest_addoption(parser):
+    parser.addoption("--emu-sanitize", action="store_true", default=False,
+                     help="build the host emulation of the library with AddressSanitizer and "
+                          "UBSan (the interpreter must preload their runtimes)")
+
+
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
 

@@ -95,20 +95,37 @@ def prepare(dst: Path, names: list[str]) -> None:
         out.write_text(text)
 
 
-def build_library(dst: Path) -> Path:
+SANITIZE = ["-g", "-fno-omit-frame-pointer", "-fsanitize=address,undefined",
+            "-fno-sanitize-recover=undefined"]
+
+
+def sanitizer_ok(tmp: Path) -> bool:
+    """Does the host compiler have the AddressSanitizer and UBSan runtimes?"""
+    src = tmp / "probe_san.c"
+    src.write_text("int main(void) { return 0; }\n")
+    r = subprocess.run(["gcc", *SANITIZE, str(src), "-o", str(tmp / "probe_san")],
+                       capture_output=True, text=True)
+    return r.returncode == 0
+
+
+def build_library(dst: Path, sanitize: bool = False) -> Path:
     """The library with every kernel on the host (tests/test_emulated_library.py):
     host code (topefft.c, batch.c), the auxiliary kernels, the pass dispatch,
     the mixed-radix and 4-points-per-thread kernels, and the power-of-two pass
     kernel for log2 L <= 8 in all four arithmetics (tests/emu/emu_launchers.cpp),
     and the persistent batch kernel with its graphs (one CTA, recorded launches).
     The tensor form and the allocation-free entry point are left out
-    (tests/emu/emu_rest.cpp)."""
+    (tests/emu/emu_rest.cpp).  With sanitize, every object is built with
+    AddressSanitizer and UBSan: device allocations are host heap blocks, so a
+    kernel's global access outside its buffer, a host-code overrun and a
+    buffer that Destroy does not free are all reported."""
     batch = ["fft_batch_host", "fft_batch_f64", "fft_batch_df64", "fft_batch_f32", "fft_batch_df32"]
     prepare(dst, ["fft_arith.cuh", "fft_pass.cuh", "fft_mixed.cuh", "fft_batch.cuh", "tfft_abi.h",
                   "fft_mixed_consts.inc", "topefft_internal.h", "fft_aux.cu", "fft_dispatch.cu",
                   "fft_inst_mixed.cu", "fft_inst_small.cu"] + [b + ".cu" for b in batch])
-    cxx = ["g++", "-std=c++20", "-O1", "-fPIC", "-pthread", f"-I{EMU}", f"-I{dst}", f"-I{INCLUDE}"]
-    cc = ["gcc", "-std=gnu11", "-O1", "-fPIC", f"-I{dst}", f"-I{INCLUDE}"]
+    san = SANITIZE if sanitize else []
+    cxx = ["g++", "-std=c++20", "-O1", "-fPIC", "-pthread", *san, f"-I{EMU}", f"-I{dst}", f"-I{INCLUDE}"]
+    cc = ["gcc", "-std=gnu11", "-O1", "-fPIC", *san, f"-I{dst}", f"-I{INCLUDE}"]
     jobs = [cc + ["-c", str(CSRC / "topefft.c"), "-o", str(dst / "topefft.o")],
             cc + ["-c", str(CSRC / "batch.c"), "-o", str(dst / "batch.o")]]
     for name in ["fft_aux", "fft_dispatch", "fft_inst_mixed", "fft_inst_small"] + batch:
@@ -127,5 +144,5 @@ def build_library(dst: Path) -> Path:
         list(ex.map(run, jobs))
     lib = dst / "libtopefft_emu.so"
     objs = [str(p) for p in sorted(dst.glob("*.o"))]
-    run(["g++", "-shared", "-pthread", "-o", str(lib), *objs])
+    run(["g++", "-shared", "-pthread", *san, "-o", str(lib), *objs])
     return lib

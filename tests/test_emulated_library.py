@@ -2,8 +2,10 @@
 pass dispatch, and the power-of-two (log2 L <= 8, and the 4-points-per-thread
 shape), mixed-radix and real-data kernels, all built from the repository's
 own sources for the host (tests/emu/emu_build.py), each kernel launch run as
-one CTA after another with one std::thread per CUDA thread.  The tensor form,
-the persistent batch kernel and CUDA graphs are not built for the host.
+one CTA after another with one std::thread per CUDA thread; the persistent
+batch kernel runs as a single CTA and a captured graph as its recorded
+launches.  The tensor form and the allocation-free entry point are not built
+for the host.
 
 The tests call the public C entry points through the same ctypes mirror as
 the GPU tests and compare with the oracle: one- and multi-pass power-of-two
@@ -21,12 +23,14 @@ import emu_build  # noqa: E402
 
 
 @pytest.fixture(scope="module")
-def E(T, tmp_path_factory):
-    """The package's ctypes mirror, bound to the host build of the library."""
+def E(T, tmp_path_factory, pytestconfig):
+    """The package's ctypes mirror, bound to the host build of the library
+    (with sanitizers under --emu-sanitize, see tests/test_sanitized_library.py)."""
     d = tmp_path_factory.mktemp("emulib")
     if not emu_build.host_cxx_ok(d):
         pytest.skip("no C++20 host compiler (std::barrier)")
-    lib = T.load_library(emu_build.build_library(d))
+    sanitize = pytestconfig.getoption("--emu-sanitize")
+    lib = T.load_library(emu_build.build_library(d, sanitize=sanitize))
     saved = T.topefft.lib
     T.topefft.lib = lib
     yield T
