@@ -97,7 +97,8 @@ void tope1DBatchPlanInit(struct topeFFT *f, struct topePlan1D *t, int x, int bat
  * (x[2j] + i x[2j+1]) plus one pre/post pass with W_x^k twiddles. */
 void tope1DUploadSpectrum(struct topeFFT *f, struct topePlan1D *t, const double *spec);
 /* tope2DPlanInit / tope3DPlanInit with type R2C (x even; x/2, y and z
- * products of 2, 3, 5, 7, 11, 13): x*y(*z) reals in, x fastest; Exec(FORWARD) writes the (x/2 + 1)*y(*z)
+ * products of 2, 3, 5, 7, 11, 13): x*y(*z) reals in, x fastest;
+ * Exec(FORWARD) writes the (x/2 + 1)*y(*z)
  * complex outputs X[kx][ky][kz], kx <= x/2, kx fastest, so d must hold
  * (x + 2)*y(*z) doubles; Exec(INVERSE) returns the reals scaled by
  * 1/(x*y*z).  The rows along x are a batched 1D real-data transform, then
@@ -108,7 +109,9 @@ void tope3DUploadSpectrum(struct topeFFT *f, struct topePlan3D *t, const double 
 
 /* ---- split-precision form: FP32 complex data ----------------------------- */
 /* Same plans and semantics as the FP64 entry points, with interleaved FP32
- * complex data (half the memory traffic).  Twiddle factors and the radix-16
+ * complex data (half the memory traffic), for lengths whose prime factors are
+ * all at most 13 (others, the DFT and Bluestein paths, are FP64 only:
+ * TOPE_ERR_INVALID_SIZE).  Twiddle factors and the radix-16
  * constants are FP64-accurate (hi, lo) FP32 pairs from FP64 sincospi.
  * Two arithmetics, chosen by topeSetSplitMode before the plan is made:
  *   TOPE_SPLIT_ACCURATE (default): double-float butterflies on chip, so only
@@ -215,7 +218,8 @@ void topeSetPassTiming(struct topeFFT *f, int enable);
 /* Writes up to max per-pass totals (ns) and launch counts; returns the
  * plan's number of passes.  For a Bluestein plan (a length of 128 points or
  * more with a prime factor above 13) these are the passes of its
- * sub-transforms (run twice per transform), as for topePassInfo. */
+ * sub-transforms (run twice per transform), as for topePassInfo; for a 2D or
+ * 3D real-data plan, the passes of its rows along x. */
 int topePassTimes(struct topeFFT *f, void *impl, uint64_t *ns, uint64_t *launches, int max);
 void topeResetPassTimes(struct topeFFT *f, void *impl);
 /* Geometry of pass i of a plan: {log2 L (or -L for a line length L that is

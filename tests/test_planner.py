@@ -4,7 +4,11 @@ built through the public entry points and their pass structure is read back
 with topePassInfo, with no GPU.  Covers the decisions the GPU tests rely on:
 one pass or a four-step split, three-pass lines, the small-transform shape,
 mixed-radix splits, the Bluestein sub-transform size, real-data row plans and
-the tensor form's tiles."""
+the tensor form's tiles, and plans of up to 2^33 points in every form.
+
+The host code is built with UndefinedBehaviorSanitizer where the compiler has
+its runtime: a signed overflow, an out-of-range shift or a misaligned access in
+the planner is reported on stderr, and every test here fails on such a report."""
 import ctypes as C
 import subprocess
 
@@ -13,15 +17,33 @@ import pytest
 
 from conftest import ROOT
 
+UBSAN = ["-fsanitize=undefined"]
+
+
+def ubsan_ok(tmp):
+    src = tmp / "probe_ub.c"
+    src.write_text("int main(void) { return 0; }\n")
+    return subprocess.run(["gcc", *UBSAN, str(src), "-o", str(tmp / "probe_ub")],
+                          capture_output=True).returncode == 0
+
 
 @pytest.fixture(scope="module")
 def S(T, tmp_path_factory):
-    out = tmp_path_factory.mktemp("stub") / "libtopefft_stub.so"
+    d = tmp_path_factory.mktemp("stub")
+    out = d / "libtopefft_stub.so"
     csrc = ROOT / "tope-fft_gb300" / "csrc"
-    subprocess.run(["gcc", "-O1", "-fPIC", "-shared", "-std=gnu11", f"-I{csrc}",
+    san = UBSAN if ubsan_ok(d) else []
+    subprocess.run(["gcc", "-O1", "-g", "-fPIC", "-shared", "-std=gnu11", *san, f"-I{csrc}",
                     f"-I{ROOT / 'include'}", str(csrc / "topefft.c"), str(csrc / "batch.c"),
                     str(ROOT / "tests" / "drivers" / "abi_stub.c"), "-o", str(out)], check=True)
     return T.load_library(out)
+
+
+@pytest.fixture(autouse=True)
+def no_ubsan_report(capfd):
+    yield
+    err = capfd.readouterr().err
+    assert "runtime error" not in err, err[-2000:]
 
 
 @pytest.fixture
@@ -242,3 +264,85 @@ def test_bluestein_runs_the_convolution_both_ways(T, S, fw, dir_, flags):
     assert fw.error == T.TOPE_SUCCESS
     launches = [r for r in call_log(S) if r[0] == 1]
     assert [r[7] for r in launches] == flags
+
+
+# ---------------------------------------------------------------- the largest plans
+BIG = 1 << 31
+
+
+def smooth(n):
+    for p in (2, 3, 5, 7, 11, 13):
+        while n % p == 0:
+            n //= p
+    return n == 1
+
+
+@pytest.mark.parametrize("f32,real,dims,batch,status", [
+    (0, 0, (1 << 30, 1, 1), 1, 0),            # three power-of-two passes
+    (0, 0, (BIG - 1, 1, 1), 1, 0),            # prime: Bluestein over 2^32 points
+    (0, 0, (3 ** 19, 1, 1), 1, 0),            # three mixed-radix passes
+    (0, 0, (1000, 1, 1), 1 << 21, 0),         # 2^31 points in short rows
+    (0, 0, (2, 1, 1), 1 << 30, 0),
+    (0, 0, (65536, 32768, 1), 1, 0),
+    (0, 0, (46656, 46656, 1), 1, 0),          # 6^6 sides
+    (0, 0, (2048, 2048, 1024), 1, 0),         # 2^32 points
+    (0, 0, (1, 2, 1 << 30), 1, 0),            # length-1 and length-2 axes
+    (0, 0, (1536, 1536, 1536), 1, 0),         # 3.6e9 points, mixed radix
+    (1, 0, (1 << 30, 1, 1), 1, 0),
+    (1, 0, (3 ** 19, 1, 1), 1, 0),
+    (1, 0, (BIG - 1, 1, 1), 1, 1),            # FP32 storage: no Bluestein
+    (1, 0, (2048, 2048, 2048), 1, 0),         # 2^33 points (64 GB of FP32)
+    (0, 1, (BIG - 2, 1, 1), 1, 0),            # real rows of 2^30 - 1 complex points
+    (0, 1, (2, 1, 1), 1 << 30, 0),            # one complex point per row: no pass
+    (0, 1, (65536, 32768, 1), 1, 0),
+    (0, 1, (1536, 1536, 1536), 1, 0),
+    (1, 1, (BIG - 2, 1, 1), 1, 1),
+    (1, 1, (2048, 2048, 2048), 1, 0),
+], ids=lambda v: str(v))
+def test_largest_plans(T, S, fw, f32, real, dims, batch, status):
+    """Plans of 2^31 to 2^33 points (int-sized sides, 64-bit totals): the
+    status, and for every pass a grid that fits a launch (at most 2^31 - 1
+    CTAs) and tiles that cover the pass's points.  Each plan also runs both
+    directions through the stand-in's launches and is destroyed."""
+    nx, ny, nz = dims
+    ndim = 1 if batch > 1 or (ny == 1 and nz == 1) else (2 if nz == 1 else 3)
+    kind = T.R2C if real else T.C2C
+    if ndim == 1:
+        t = T.TopePlan1D()
+        init = S.tope1DBatchPlanInitF32 if f32 else S.tope1DBatchPlanInit
+        init(C.byref(fw), C.byref(t), nx, batch, kind, None)
+        run, destroy = S.tope1DExecDevice, S.tope1DDestroy
+    elif ndim == 2:
+        t = T.TopePlan2D()
+        init = S.tope2DPlanInitF32 if f32 else S.tope2DPlanInit
+        init(C.byref(fw), C.byref(t), nx, ny, kind, None)
+        run, destroy = S.tope2DExecDevice, S.tope2DDestroy
+    else:
+        t = T.TopePlan3D()
+        init = S.tope3DPlanInitF32 if f32 else S.tope3DPlanInit
+        init(C.byref(fw), C.byref(t), nx, ny, nz, kind, None)
+        run, destroy = S.tope3DExecDevice, S.tope3DDestroy
+    assert fw.error == status
+    if status:
+        assert not t.impl
+        fw.error = 0
+        return
+    points = nx * ny * nz * batch
+    # the complex points each pass covers: all of them, half of them for real
+    # rows (a 2D/3D real plan's pass list is its rows along x), or the
+    # Bluestein sub-transform's M >= 2N - 1
+    covered = points // 2 if real else points
+    line = nx // 2 if real else nx
+    bluestein = ndim == 1 and not smooth(line)
+    for q in passes(S, fw, t):
+        assert 1 <= q["ctas"] <= BIG - 1, q
+        tile = q["ctas"] * q["b"] * q["len"]
+        if bluestein:
+            assert tile >= 2 * covered - 1, q
+        else:
+            assert covered <= tile < 2 * covered, q
+    for dir_ in (T.FORWARD, T.INVERSE):
+        run(C.byref(fw), C.byref(t), dir_)
+        assert fw.error == T.TOPE_SUCCESS
+    destroy(C.byref(fw), C.byref(t))
+    assert fw.error == T.TOPE_SUCCESS and not t.impl
