@@ -91,6 +91,9 @@ struct Spec {
     int post;           /* 0 none, 1 two-level table, 2 whole table */
     bool conj;          /* conj on load and store with scale 1/L: an inverse */
     double magnitude;   /* input scale */
+    long long n1 = 1;   /* groups of `lines` lines along the grid's second dimension */
+    int level = 0;      /* four-step factor from the line index (0) or the group (1),
+                           as in the middle pass of a three-pass line */
 };
 
 template <class A, class Launch>
@@ -98,7 +101,8 @@ static double run_case(const Spec &s, Launch launch)
 {
     using Store = typename A::Store;
     using TW = typename A::TW;
-    const long long L = s.L, lines = s.lines, tot = L * lines, N = L * lines;
+    const long long L = s.L, lines = s.lines, grp = L * lines, tot = grp * s.n1;
+    const long long N = L * (s.level ? s.n1 : lines); /* t * k < N for every factor */
     std::vector<Store> in(tot), out(tot);
     std::vector<CLD> x(tot);
     for (long long e = 0; e < tot; e++) {
@@ -118,14 +122,16 @@ static double run_case(const Spec &s, Launch launch)
     p.in = in.data();
     p.out = out.data();
     p.n[0] = lines;
-    p.n[1] = p.n[2] = 1;
+    p.n[1] = s.n1;
+    p.n[2] = 1;
+    p.is[1] = p.os[1] = grp;
     p.is[0] = p.os[0] = s.rows ? L : 1;
     p.ies = p.oes = s.rows ? 1 : lines;
     p.tw = tw.data();
     int shift = 0;
     if (s.post) {
         p.post_tw = 1;
-        p.tw_level = 0;
+        p.tw_level = s.level;
         p.tw_n = N;
         if (s.post == 2) {
             whole.resize(N);
@@ -148,20 +154,21 @@ static double run_case(const Spec &s, Launch launch)
     }
     launch(p);
     LD num = 0, den = 0;
-    for (long long g = 0; g < lines; g++)
-        for (long long k = 0; k < L; k++) {
-            CLD acc = 0;
-            for (long long j = 0; j < L; j++) {
-                CLD v = x[s.rows ? g * L + j : j * lines + g];
-                if (s.conj) v = std::conj(v);
-                acc += v * wpow(j * k, L);
+    for (long long h = 0; h < s.n1; h++)
+        for (long long g = 0; g < lines; g++)
+            for (long long k = 0; k < L; k++) {
+                CLD acc = 0;
+                for (long long j = 0; j < L; j++) {
+                    CLD v = x[h * grp + (s.rows ? g * L + j : j * lines + g)];
+                    if (s.conj) v = std::conj(v);
+                    acc += v * wpow(j * k, L);
+                }
+                if (s.post) acc *= wpow((s.level ? h : g) * k, N);
+                if (s.conj) acc = std::conj(acc) / (LD)L;
+                const CLD got = get(out[h * grp + (s.rows ? g * L + k : k * lines + g)]);
+                num += std::norm(got - acc);
+                den += std::norm(acc);
             }
-            if (s.post) acc *= wpow(g * k, N);
-            if (s.conj) acc = std::conj(acc) / (LD)L;
-            const CLD got = get(out[s.rows ? g * L + k : k * lines + g]);
-            num += std::norm(got - acc);
-            den += std::norm(acc);
-        }
     return (double)sqrtl(num / den);
 }
 
@@ -181,7 +188,7 @@ static void mixed(int id, const Spec &s, double tol)
         p.nrad = nr;
         std::memcpy(p.radix, rad, nr);
         smem_limit(tfft::mixed_smem_bytes((int)(s.L * s.B), (int)sizeof(typename A::S)));
-        run_grid(tfft::mixed_kernel<A>, p, (s.lines + s.B - 1) / s.B, tfft::kMixedThreads);
+        run_grid(tfft::mixed_kernel<A>, p, (s.lines + s.B - 1) / s.B * s.n1, tfft::kMixedThreads);
     });
     std::printf("case %d mixed_kernel<%d> L=%lld B=%lld rel=%.3e tol=%.1e\n", id, A::kId, s.L, s.B,
                 e, tol);
@@ -194,7 +201,7 @@ static void pass(int id, const Spec &s, double tol)
         p.log_l = LOG_L;
         p.ept = EPT == 16 ? 0 : EPT;
         smem_limit(tfft::pass_smem_bytes<A, LOG_L, B, EPT>());
-        run_grid(tfft::pass_kernel<A, LOG_L, B, EPT>, p, (s.lines + B - 1) / B,
+        run_grid(tfft::pass_kernel<A, LOG_L, B, EPT>, p, (s.lines + B - 1) / B * s.n1,
                  tfft::Shape<LOG_L, EPT>::TPL * B);
     });
     std::printf("case %d pass_kernel<%d,%d,%d,%d> rel=%.3e tol=%.1e\n", id, A::kId, LOG_L, B, EPT,
@@ -218,5 +225,9 @@ int main(int argc, char **argv)
     if (want(9)) pass<ArithDF64, 8, 8, 16>(9, {256, 8, 16, false, 1, false, 1.0}, 1e-13);
     if (want(10)) pass<ArithF32, 9, 8, 16>(10, {512, 8, 16, true, 0, false, 1.0}, 3e-7);
     if (want(11)) pass<ArithDF64, 12, 2, 16>(11, {4096, 2, 2, true, 0, true, 1e300}, 1e-13);
+    /* the middle pass of a three-pass line: 3 groups, factor W_N^(group * k) */
+    if (want(12)) mixed<ArithF64>(12, {243, 2, 3, false, 1, false, 1.0, 3, 1}, 1e-14);
+    if (want(13)) mixed<ArithDF64>(13, {81, 4, 5, true, 2, true, 1.0, 3, 1}, 1e-13);
+    if (want(14)) pass<ArithF64, 8, 2, 16>(14, {256, 2, 3, false, 1, false, 1.0, 4, 1}, 1e-14);
     return 0;
 }

@@ -6,7 +6,9 @@ barrier-based reductions, __shared__ arrays shared by the CTA's threads.  The
 driver (tests/emu/emu_driver.cpp) transforms a few lines per case, in the
 power-of-two kernel (16 and 4 points per thread) and the mixed-radix kernel,
 for every arithmetic, with row and strided layouts, two-level and whole
-four-step tables, inverse conjugation and scale, and double-float tiles that
+four-step tables indexed by the line or (the middle pass of a three-pass
+line) by the group along the grid's second dimension, inverse conjugation
+and scale, and double-float tiles that
 take the 2^600 lift, and compares with a long-double DFT of the same lines.
 This checks the kernels' index arithmetic and butterflies without a GPU; the
 GPU tests check the compiled device code.
@@ -28,7 +30,7 @@ from conftest import ROOT
 CSRC = ROOT / "tope-fft_gb300" / "csrc"
 EMU = ROOT / "tests" / "emu"
 HEADERS = ["fft_pass.cuh", "fft_mixed.cuh", "fft_arith.cuh", "tfft_abi.h", "fft_mixed_consts.inc"]
-NCASES = 12
+NCASES = 15
 NAUX = 7
 
 
@@ -116,7 +118,7 @@ def emu_san(tmp_path_factory, emu):
     return exe
 
 
-@pytest.mark.parametrize("case", [0, 2, 3, 4, 5, 6, 7, 9, 10])
+@pytest.mark.parametrize("case", [0, 2, 3, 4, 5, 6, 7, 9, 10, 12, 14])
 def test_kernel_under_sanitizers(emu_san, case):
     r = subprocess.run([str(emu_san), str(case)], capture_output=True, text=True, timeout=600)
     assert r.returncode == 0 and "runtime error" not in r.stderr, r.stderr[-2000:]
