@@ -106,7 +106,7 @@ METRIC = "C2C GFLOP/s & HBM GB/s vs roofline, FP64 plain vs split-precision at s
 SEED0 = 0x70E0F0F7
 L2_BYTES = 129 * 10 ** 6
 FALLBACK_HBM_GBS = 6800.0
-# measured on a GB300 of this machine: DFMA 0.50 Tinstr/s (1.0 TFLOP/s)
+# measured on a GB300 (profiles/fp_pipe_rates_gb300.md): DFMA 0.50 Tinstr/s (1.0 TFLOP/s)
 FP64_PIPE_TFLOPS = 1.0
 
 
