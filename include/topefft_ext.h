@@ -219,7 +219,8 @@ void topeSetPassTiming(struct topeFFT *f, int enable);
  * plan's number of passes.  For a Bluestein plan (a length of 128 points or
  * more with a prime factor above 13) these are the passes of its
  * sub-transforms (run twice per transform), as for topePassInfo; for a 2D or
- * 3D real-data plan, the passes of its rows along x. */
+ * 3D real-data plan, the passes of its rows along x, then its y (and z)
+ * passes over the spectrum. */
 int topePassTimes(struct topeFFT *f, void *impl, uint64_t *ns, uint64_t *launches, int max);
 void topeResetPassTimes(struct topeFFT *f, void *impl);
 /* Geometry of pass i of a plan: {log2 L (or -L for a line length L that is

@@ -167,7 +167,22 @@ static void r2c(struct topeFFT *f, int ndim, int nx, int ny, int nz)
         struct topePlan2D t;
         tope2DPlanInit(f, &t, nx, ny, R2C, d);
         CHECK(f->error == 0, "2D R2C plan %dx%d: status %d", nx, ny, f->error);
+        /* the pass list: the rows along x, then the y pass over the spectrum,
+         * each launched once per direction */
+        topeSetPassTiming(f, 1);
         tope2DExec(f, &t, d, FORWARD);
+        uint64_t ns[8], launches[8];
+        int np = topePassTimes(f, t.impl, ns, launches, 8);
+        int64_t info[6] = {0};
+        long long last = 0; /* the last pass's line length */
+        if (np >= 2 && np <= 8 && topePassInfo(f, t.impl, np - 1, info) == 0)
+            last = info[0] < 0 ? -info[0] : (info[0] < 62 ? 1LL << info[0] : 0);
+        CHECK(last == ny, "2D R2C pass list: %d passes, last of length %lld", np, last);
+        for (int i = 0; i < np && i < 8; i++)
+            CHECK(launches[i] == 1, "2D R2C pass %d: %llu launches", i,
+                  (unsigned long long)launches[i]);
+        topeResetPassTimes(f, t.impl);
+        topeSetPassTiming(f, 0);
         tope2DExec(f, &t, d, INVERSE);
         tope2DDestroy(f, &t);
     } else {

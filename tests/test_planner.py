@@ -149,10 +149,20 @@ def test_nd_rejects_large_prime_sides(T, S, fw):
 def test_real_plans_transform_half_length_rows(T, S, fw):
     p = passes(S, fw, plan1d(T, S, fw, 2000, real=True))
     assert [q["len"] for q in p] == [1000]
+    # 2D: the rows (50 complex points each), then the y pass over the
+    # 51-column spectrum, 51 lines of 60 points
     t = T.TopePlan2D()
     S.tope2DPlanInit(C.byref(fw), C.byref(t), 100, 60, T.R2C, None)
     assert fw.error == T.TOPE_SUCCESS
-    assert [q["len"] for q in passes(S, fw, t)] == [50]
+    p = passes(S, fw, t)
+    assert [q["len"] for q in p] == [50, 60]
+    assert p[1]["ctas"] * p[1]["b"] >= 51
+    assert S.topePassInfo(C.byref(fw), t.impl, 2, (C.c_int64 * 6)()) == -1
+    fw.error = 0
+    t3 = T.TopePlan3D()
+    S.tope3DPlanInit(C.byref(fw), C.byref(t3), 16, 12, 10, T.R2C, None)
+    assert fw.error == T.TOPE_SUCCESS
+    assert [q["len"] for q in passes(S, fw, t3)] == [8, 12, 10]
 
 
 def test_split_precision_shapes(T, S, fw):
@@ -329,8 +339,8 @@ def test_largest_plans(T, S, fw, f32, real, dims, batch, status):
         return
     points = nx * ny * nz * batch
     # the complex points each pass covers: all of them, half of them for real
-    # rows (a 2D/3D real plan's pass list is its rows along x), or the
-    # Bluestein sub-transform's M >= 2N - 1
+    # rows (at least that for the y/z passes over the x/2 + 1 spectrum
+    # columns), or the Bluestein sub-transform's M >= 2N - 1
     covered = points // 2 if real else points
     line = nx // 2 if real else nx
     bluestein = ndim == 1 and not smooth(line)

@@ -1900,39 +1900,64 @@ static tope_impl *passes_of(tope_impl *P)
     return (P && P->mode == MODE_BLUESTEIN && P->sub) ? P->sub : P;
 }
 
+/* The plans whose passes a plan's pass list shows, in execution order: the
+ * plan (or its Bluestein sub-plan), then, for a 2D/3D real-data plan, the
+ * spectrum plan's y/z passes.  Returns how many (0 for no plan). */
+static int pass_plans(tope_impl *P, tope_impl *out[2])
+{
+    if (!P) return 0;
+    out[0] = passes_of(P);
+    out[1] = P->specp;
+    return out[1] ? 2 : 1;
+}
+
 int topePassTimes(struct topeFFT *f, void *impl, uint64_t *ns, uint64_t *launches, int max)
 {
-    tope_impl *P = passes_of(impl_of(f, impl));
-    if (!P) return -1;
+    tope_impl *Q[2];
+    const int nq = pass_plans(impl_of(f, impl), Q);
+    if (!nq) return -1;
     int rc = tfft_stream_sync(f->command_queue);
     if (rc) {
         cuda_status(f, rc);
         return -1;
     }
-    pev_settle(P);
-    for (int i = 0; i < P->npass && i < max; i++) {
-        if (ns) ns[i] = P->pass_ns[i];
-        if (launches) launches[i] = P->pass_launches[i];
+    int k = 0;
+    for (int q = 0; q < nq; q++) {
+        pev_settle(Q[q]);
+        for (int i = 0; i < Q[q]->npass; i++, k++)
+            if (k < max) {
+                if (ns) ns[k] = Q[q]->pass_ns[i];
+                if (launches) launches[k] = Q[q]->pass_launches[i];
+            }
     }
     set_status(f, TOPE_SUCCESS);
-    return P->npass;
+    return k;
 }
 
 void topeResetPassTimes(struct topeFFT *f, void *impl)
 {
-    tope_impl *P = passes_of(impl_of(f, impl));
-    if (!P) return;
+    tope_impl *Q[2];
+    const int nq = pass_plans(impl_of(f, impl), Q);
+    if (!nq) return;
     tfft_stream_sync(f->command_queue);
-    P->pev_used = 0;
-    memset(P->pass_ns, 0, sizeof(P->pass_ns));
-    memset(P->pass_launches, 0, sizeof(P->pass_launches));
+    for (int q = 0; q < nq; q++) {
+        Q[q]->pev_used = 0;
+        memset(Q[q]->pass_ns, 0, sizeof(Q[q]->pass_ns));
+        memset(Q[q]->pass_launches, 0, sizeof(Q[q]->pass_launches));
+    }
     set_status(f, TOPE_SUCCESS);
 }
 
 int topePassInfo(struct topeFFT *f, void *impl, int i, int64_t info[6])
 {
-    tope_impl *P = passes_of(impl_of(f, impl));
-    if (!P || !info) return -1;
+    tope_impl *Q[2];
+    const int nq = pass_plans(impl_of(f, impl), Q);
+    if (!nq || !info) return -1;
+    tope_impl *P = Q[0];
+    if (nq == 2 && i >= Q[0]->npass) {
+        i -= Q[0]->npass;
+        P = Q[1];
+    }
     if (i < 0 || i >= P->npass) {
         set_status(f, TOPE_ERR_INVALID_ARG);
         return -1;
