@@ -72,9 +72,14 @@ def test_struct_layout_matches_mirror(T, tmp_path):
         assert int(val) == want, (cname, field, val, want)
 
 
-def test_reference_style_driver_links(T, tmp_path):
-    exe = tmp_path / "tope_driver"
-    r = subprocess.run(["gcc", "-O2", f"-I{INCLUDE}", str(ROOT / "tests" / "drivers" / "tope_driver.c"),
+@pytest.mark.parametrize("driver", ["tope_driver", "ext_driver"])
+def test_c_drivers_link(T, tmp_path, driver):
+    """The reference-style caller and the caller of the whole extension
+    surface compile without warnings against include/ and link against the
+    built library."""
+    exe = tmp_path / driver
+    r = subprocess.run(["gcc", "-O2", "-Wall", "-Werror", f"-I{INCLUDE}",
+                        str(ROOT / "tests" / "drivers" / f"{driver}.c"),
                         "-o", str(exe), f"-L{T.LIB_PATH.parent}", "-ltopefft",
                         f"-Wl,-rpath,{T.LIB_PATH.parent}", "-lm"], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
