@@ -462,3 +462,30 @@ def test_random_plans(E, orc, seed):
         E.topeFFTDestroy(f)
         checked += 1
     assert checked >= 6
+
+
+def test_binding_refuses_short_output_arrays(E, orc):
+    """The Python binding checks a numpy array against what an Exec writes
+    before the C code runs: the plan's data, or for a real-data plan's
+    forward transform its x/2 + 1 complex outputs per row."""
+    f = E.TopeFFT()
+    E.topeFFTInit(f)
+    n, rows = 64, 3
+    x = orc.uniform(n * rows // 2, SEED0 + 91)
+    t = E.TopePlan1D()
+    E.tope1DBatchPlanInit(f, t, n, rows, E.R2C, x)
+    E.check(f)
+    with pytest.raises(ValueError):
+        E.tope1DExec(f, t, np.zeros(n * rows), E.FORWARD)  # reals-sized: too short
+    spec = np.zeros((n + 2) * rows)
+    E.tope1DExec(f, t, spec, E.FORWARD)
+    E.check(f)
+    E.tope1DExec(f, t, np.zeros(n * rows), E.INVERSE)  # the inverse writes the reals
+    E.check(f)
+    E.tope1DDestroy(f, t)
+    c = E.TopePlan2D()
+    E.tope2DPlanInit(f, c, 8, 4, E.C2C, np.zeros(64))
+    with pytest.raises(ValueError):
+        E.tope2DExec(f, c, np.zeros(63), E.FORWARD)
+    E.tope2DDestroy(f, c)
+    E.topeFFTDestroy(f)

@@ -203,6 +203,20 @@ def _need(d, x, rows, type_) -> None:
             raise ValueError(f"data holds {d.size} values, the plan reads {want}")
 
 
+def _need_out(d, t, dir_) -> None:
+    """A host array handed to an Exec receives what the transform writes:
+    the plan's dataSize bytes, or for a real-data plan's forward transform
+    its spectrum, (x + 2)/x times the reals.  Checked only for numpy arrays
+    and live plans (the library reports the rest with a status)."""
+    if not isinstance(d, np.ndarray) or not t.impl or not t.dataSize:
+        return
+    want = t.dataSize
+    if t.type == R2C and dir_ == FORWARD and t.x > 0:
+        want = t.dataSize // t.x * (t.x + 2)
+    if d.nbytes < want:
+        raise ValueError(f"data holds {d.nbytes} bytes, the transform writes {want}")
+
+
 def topeFFTInit(f: TopeFFT) -> None:
     lib.topeFFTInit(C.byref(f))
 
@@ -238,6 +252,7 @@ def tope1DBatchPlanInit(f, t, x, batch, type_, d) -> None:
 
 
 def tope1DExec(f, t, d, dir_) -> None:
+    _need_out(d, t, dir_)
     lib.tope1DExec(C.byref(f), C.byref(t), _ptr(d), dir_)
 
 
@@ -251,6 +266,7 @@ def tope2DPlanInit(f, t, x, y, type_, d) -> None:
 
 
 def tope2DExec(f, t, d, dir_) -> None:
+    _need_out(d, t, dir_)
     lib.tope2DExec(C.byref(f), C.byref(t), _ptr(d), dir_)
 
 
@@ -272,6 +288,7 @@ def tope3DPlanInit(f, t, x, y, z, type_, d) -> None:
 
 
 def tope3DExec(f, t, d, dir_) -> None:
+    _need_out(d, t, dir_)
     lib.tope3DExec(C.byref(f), C.byref(t), _ptr(d), dir_)
 
 
@@ -366,6 +383,7 @@ def tope3DPlanInitF32(f, t, x, y, z, type_, d) -> None:
 def execF32(f, t, d, dir_) -> None:
     fn = {TopePlan1D: lib.tope1DExecF32, TopePlan2D: lib.tope2DExecF32,
           TopePlan3D: lib.tope3DExecF32}[type(t)]
+    _need_out(d, t, dir_)
     fn(C.byref(f), C.byref(t), _fptr(d), dir_)
 
 
@@ -393,6 +411,8 @@ def topeBatchPlanInit(f, b, nx, ny, type_, d) -> None:
 
 
 def topeBatchExec(f, b, d, dir_) -> None:
+    if isinstance(d, np.ndarray) and b.impl and d.nbytes < b.dataSize:
+        raise ValueError(f"data holds {d.nbytes} bytes, the batch writes {b.dataSize}")
     if d is not None and np.asarray(d).dtype == np.float32:
         lib.topeBatchExecF32(C.byref(f), C.byref(b), _fptr(d), dir_)
     else:
