@@ -239,9 +239,11 @@ int topePassInfo(struct topeFFT *f, void *impl, int i, int64_t info[6]);
  * loading the library holds until exit; nothing is allocated.  n must be a
  * power of two from 1 to TOPE_NOALLOC_MAX_N, else TOPE_ERR_INVALID_SIZE.
  * The first call on a device builds the tables and waits for the stream:
- * make it before any stream capture.  All calls share one scratch array, so
- * calls whose kernels may overlap on the GPU race: serialise them.
- * Returns a topeStatus. */
+ * make it before any stream capture.  The tables belong to the device's
+ * context as it was at that first call: after cudaDeviceReset the entry
+ * point must not be called again in the same process.  All calls share one
+ * scratch array, so calls whose kernels may overlap on the GPU race:
+ * serialise them.  Returns a topeStatus. */
 #define TOPE_NOALLOC_MAX_N (1 << 20)
 int topeExec1DNoAlloc(const double *d_in, double *d_out, int n, int dir, void *stream);
 

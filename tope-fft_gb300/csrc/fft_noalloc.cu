@@ -11,17 +11,25 @@
  * until the process exits:
  *   g_na_scratch   the four-step intermediate, 2^20 complex doubles (16 MiB)
  *   g_na_wl        the W_L twiddle tables for L = 2^1 .. 2^13
- *   g_na_fs        the four-step factor tables for n = 2^14 .. 2^20
+ *   g_na_fs        the four-step factor tables for n = 2^10 .. 2^20
  * Lengths are powers of two from 1 to 2^20 (TOPE_NOALLOC_MAX_N); anything
  * else is rejected with TOPE_ERR_INVALID_SIZE before any work is queued.
+ * Up to 2^9 points the transform is one pass; from 2^10 on it is two
+ * four-step passes (short passes with 4 points per thread), the split the
+ * allocating path makes for a single line of that length.
  *
  * Set-up: the first call on each device computes the tables with that
  * device current, queued on the caller's stream, and waits for that stream
  * to finish, so make the first call before any stream capture.  Later calls
- * only queue kernels.  Nothing in the scratch has to start at zero: the
- * first pass writes every element the second pass reads.  All calls share
- * the one scratch array, so calls whose kernels overlap on the GPU (two
- * streams, or two host threads) race on it; serialise them.
+ * only queue kernels.  The set-up is published with a release store and read
+ * with an acquire load, so a thread that sees it finished also sees the
+ * device addresses it resolved.  Those addresses and tables belong to the
+ * device's context as it was at set-up: after cudaDeviceReset (or any other
+ * teardown of the primary context) the entry point must not be called again
+ * in that process.  Nothing in the scratch has to start at zero: the first
+ * pass writes every element the second pass reads.  All calls share the one
+ * scratch array, so calls whose kernels overlap on the GPU (two streams, or
+ * two host threads) race on it; serialise them.
  */
 #include <cuda_runtime.h>
 #include <pthread.h>
@@ -32,7 +40,7 @@
 
 #define NA_MAX_LOG 20
 #define NA_MAX_LOG_L 13
-#define NA_FS_MIN_LOG 14
+#define NA_FS_MIN_LOG 10
 #define NA_FS_ENTRIES 2048 /* 2^shift + 2^(log n - shift) <= 2 * 2^10 */
 
 static __device__ __align__(256) double2 g_na_scratch[1 << NA_MAX_LOG];
@@ -42,7 +50,7 @@ static __device__ __align__(256) double2 g_na_fs[NA_MAX_LOG - NA_FS_MIN_LOG + 1]
 #define NA_MAX_DEVICES 64
 
 typedef struct na_dev {
-    int ready;
+    int ready; /* 1 once set-up finished: release store, acquire load */
     double2 *scratch, *wl, *fs;
 } na_dev;
 
@@ -71,8 +79,33 @@ static int na_setup(int dev, cudaStream_t s)
             return TOPE_ERR_CUDA;
     }
     if (cudaStreamSynchronize(s) != cudaSuccess) return TOPE_ERR_CUDA;
-    d->ready = 1;
+    __atomic_store_n(&d->ready, 1, __ATOMIC_RELEASE);
     return TOPE_SUCCESS;
+}
+
+/* lines per CTA for a pass of `lines` strided lines of 2^log_l points and
+ * ept points per thread: the allocating planner's rule (about 256 threads,
+ * at least 8 adjacent lines, at most 8192 points per CTA, 4096 with 4
+ * points per thread), narrowed until the pass has at least 32 CTAs */
+static int na_lines_per_cta(int log_l, int64_t lines, int ept)
+{
+    const int64_t L = (int64_t)1 << log_l;
+    const int64_t e = L < ept ? L : ept;
+    int64_t want = 256 * e / L;
+    if (want < 8) want = 8;
+    int64_t maxb = (ept == 4 ? 4096 : 8192) / L;
+    if (maxb > 32) maxb = 32;
+    if (want > maxb) want = maxb;
+    if (want > lines) want = lines;
+    if (want < 1) want = 1;
+    while (want > 1 && lines / want < 32) want >>= 1;
+    return (int)want;
+}
+
+/* 4 points per thread for short passes of at most 2^16 points */
+static int na_ept(int log_l, int64_t points)
+{
+    return log_l >= 2 && log_l <= 7 && points <= 65536 ? 4 : 0;
 }
 
 static void na_pass_init(tfft_pass *p, int log_l, const double2 *tw)
@@ -94,9 +127,10 @@ extern "C" int topeExec1DNoAlloc(const double *d_in, double *d_out, int n, int d
     cudaStream_t s = (cudaStream_t)stream;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= NA_MAX_DEVICES) return TOPE_ERR_CUDA;
-    if (!g_na[dev].ready) {
+    if (!__atomic_load_n(&g_na[dev].ready, __ATOMIC_ACQUIRE)) {
         pthread_mutex_lock(&g_na_lock);
-        int st = g_na[dev].ready ? TOPE_SUCCESS : na_setup(dev, s);
+        int st = __atomic_load_n(&g_na[dev].ready, __ATOMIC_ACQUIRE) ? TOPE_SUCCESS
+                                                                     : na_setup(dev, s);
         pthread_mutex_unlock(&g_na_lock);
         if (st) return st;
     }
@@ -104,13 +138,14 @@ extern "C" int topeExec1DNoAlloc(const double *d_in, double *d_out, int n, int d
     const int inv = dir == INVERSE;
     const double scale = inv ? 1.0 / (double)n : 1.0;
     tfft_pass p = {0};
-    if (lg <= NA_MAX_LOG_L) {
+    if (lg < NA_FS_MIN_LOG) {
         /* one pass, input to output */
         na_pass_init(&p, lg, d->wl + ((size_t)1 << lg));
         p.in = d_in;
         p.out = d_out;
         p.ies = p.oes = 1;
         p.b_tile = 1;
+        p.ept = na_ept(lg, n);
         p.conj_in = p.conj_out = inv;
         p.scale = scale;
         return tfft_launch_pass(&p, stream) ? TOPE_ERR_CUDA : TOPE_SUCCESS;
@@ -127,7 +162,8 @@ extern "C" int topeExec1DNoAlloc(const double *d_in, double *d_out, int n, int d
     p.ies = p.oes = n1;
     p.n[0] = n1;
     p.is[0] = p.os[0] = 1;
-    p.b_tile = 8;
+    p.ept = na_ept(l2, n);
+    p.b_tile = na_lines_per_cta(l2, n1, p.ept ? 4 : 16);
     p.conj_in = inv;
     p.post_tw = 1;
     p.tw_level = 0;
@@ -145,7 +181,8 @@ extern "C" int topeExec1DNoAlloc(const double *d_in, double *d_out, int n, int d
     q.n[0] = n2;
     q.is[0] = n1;
     q.os[0] = 1;
-    q.b_tile = 8;
+    q.ept = na_ept(l1, n);
+    q.b_tile = na_lines_per_cta(l1, n2, q.ept ? 4 : 16);
     q.conj_out = inv;
     q.scale = scale;
     return tfft_launch_pass(&q, stream) ? TOPE_ERR_CUDA : TOPE_SUCCESS;
