@@ -207,6 +207,47 @@ def p_min(n: int, fp32: bool = False) -> int:
 
 
 # ------------------------------------------------------------------ helpers
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu, else /proc/cpuinfo, else the
+    platform string)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.split(":", 1)[0].strip() == "Model name":
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        for line in Path("/proc/cpuinfo").read_text().splitlines():
+            if line.lower().startswith(("model name", "cpu model")):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    import platform
+    return platform.processor() or platform.machine()
+
+
+def workload_config(args, wl: dict) -> dict:
+    """The `config` object of a bench line: the workload alone, identical in
+    both arms (what computes it is described outside `config`)."""
+    if wl.get("uneven"):
+        nx, ny = uneven_shapes(n1d=wl.get("n1d", 20000), n2d=wl.get("n2d", 500))
+        total = sum(a * b for a, b in zip(nx, ny))
+        es = 8 if wl.get("f32") else 16
+        extra = {"transforms": len(nx)}
+    else:
+        nx_, ny_, nz_ = wl["dims"]
+        total = nx_ * ny_ * nz_ * wl["batch"]
+        es = 8 if wl.get("f32") else 16
+        extra = {}
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    return dict({"workload": args.workload, "description": wl["desc"], "points": total},
+                **extra,
+                l2=(f"inputs larger than L2 ({total * es >> 20} MiB array vs 129 MB L2)"
+                    if total * es > L2_BYTES else "array fits in L2 (latency-bound size)"),
+                parallelism=f"replicas x{ws}")
+
+
 def measured_peaks() -> tuple[float, str]:
     p = ROOT / "MEASURED_PEAKS.json"
     try:
@@ -340,7 +381,8 @@ def cpu_reference_rate(wl: dict, budget_s: float = 30.0, steps: int = 1, warmup:
         sample = (f"the reference DFT (O(n^2)) at n={n_s}, forward, {t_s:.3f} s on {cores} threads, "
                   f"scaled by (n/{n_s})^2 to n={n_all} and doubled for the inverse")
         return gflops, {"value": sig(gflops), "unit": "GFLOP/s", "cores": cores,
-                        "kind": kind, "sample": sample, "ms_per_step": t * 1e3}
+                        "cpu_model": cpu_model(), "kind": kind, "sample": sample,
+                        "ms_per_step": t * 1e3}
     if wl.get("real"):
         # the reference has no real-data path: its complex transform of the
         # reals with zero imaginary parts
@@ -379,8 +421,9 @@ def cpu_reference_rate(wl: dict, budget_s: float = 30.0, steps: int = 1, warmup:
     gflops = flops / t / 1e9
     sample = (f"{'x'.join(map(str, sample_dims))} x batch {sample_batch}, forward+inverse, "
               f"{len(times)} timed step(s), median {t:.3f} s, {cores} threads")
-    return gflops, {"value": sig(gflops), "unit": "GFLOP/s", "cores": cores, "kind": kind,
-                    "sample": sample, "ms_per_step": t * 1e3}
+    return gflops, {"value": sig(gflops), "unit": "GFLOP/s", "cores": cores,
+                    "cpu_model": cpu_model(), "kind": kind, "sample": sample,
+                    "ms_per_step": t * 1e3}
 
 
 # ------------------------------------------------------------------ GPU leg
@@ -479,11 +522,18 @@ def run_gpu(args, wl: dict) -> dict:
     xs64 = xs.astype(np.float64)
     rt = float(np.sqrt(np.sum((back.astype(np.float64) - xs64) ** 2) / np.sum(xs64 * xs64)))
     accuracy = None
-    if f32:
-        # one forward transform against the library's own FP64 path on the
-        # FP64 input (before FP32 rounding)
-        T.uploadF32(f, t, xs)
-        T.execF32(f, t, back, T.FORWARD)
+    if (f32 or args.arith == "df64") and not real:
+        # one forward transform against the library's own native-FP64 path on
+        # the FP64 input (before FP32 rounding for FP32 data); that path is
+        # parity-tested against the oracle by the GPU tests
+        if f32:
+            T.uploadF32(f, t, xs)
+            T.execF32(f, t, back, T.FORWARD)
+        else:
+            T.upload(f, t, xs)
+            {T.TopePlan1D: T.tope1DExec, T.TopePlan2D: T.tope2DExec,
+             T.TopePlan3D: T.tope3DExec}[type(t)](f, t, back, T.FORWARD)
+        T.check(f)
         saved = f.arith
         T.topeSetArith(f, T.TOPE_ARITH_FP64)
         ref = x.copy()
@@ -497,8 +547,10 @@ def run_gpu(args, wl: dict) -> dict:
         accuracy = {"rel_l2_vs_fp64": float(np.sqrt(np.sum((got - ref) ** 2) / np.sum(ref * ref))),
                     "max_abs_vs_fp64": float(np.max(np.abs(got - ref))),
                     "max_abs_ref": float(np.max(np.abs(ref))),
-                    "reference": "the library's native-FP64 path on the FP64 input, forward",
-                    "gate": 1e-7}
+                    "reference": ("the library's native-FP64 path on the same FP64 input, one "
+                                  "forward transform (that path is checked against the oracle "
+                                  "by the GPU tests)"),
+                    "gate": 1e-7 if f32 else 1e-13 * float(np.log2(total))}
         del ref, got
 
     # dominant kernel: the pass with the largest total time
@@ -518,6 +570,14 @@ def run_gpu(args, wl: dict) -> dict:
                 "launch_us": round(avg_ns / 1e3, 2),
                 "bytes_per_launch": bytes_per_launch,
                 "fp64_pipe_tflops_measured": FP64_PIPE_TFLOPS}
+        if not f32 and args.arith == "fp64":
+            # native FP64 is bound by the FP64 pipe: the whole step's
+            # algorithmic flops against the measured DFMA rate (2 flops each)
+            roof["fp64_pipe"] = {"achieved_gflops": round(value_gflops, 1),
+                                 "peak_gflops": FP64_PIPE_TFLOPS * 1e3,
+                                 "frac": round(value_gflops / (FP64_PIPE_TFLOPS * 1e3), 4),
+                                 "basis": "5 N log2 N per direction over the step time, "
+                                          "against the measured DFMA rate x 2"}
 
     # e2e through the C interface with pinned host buffers
     nbytes = xs.nbytes
@@ -558,7 +618,9 @@ def run_gpu(args, wl: dict) -> dict:
         arith_desc = "split precision, fast: FP32 data and butterflies, FP64-accurate hi/lo twiddles"
     elif f32 and args.split == "tensor":
         arith_desc = ("split precision, tensor: FP32 data, radix-16 stages as tcgen05 GEMMs on "
-                      "3-way BF16 splits with FP32 accumulation, FP64-accurate hi/lo twiddles")
+                      "three-piece FP16 splits (an exact leading FP32 accumulator and a "
+                      "cross-product one), double-float twiddles and exchange, FP64-accurate "
+                      "hi/lo twiddle tables")
     elif f32:
         arith_desc = ("split precision, accurate: FP32 data, double-float butterflies on chip, "
                       "FP64-accurate hi/lo twiddles")
@@ -572,11 +634,8 @@ def run_gpu(args, wl: dict) -> dict:
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32" if f32 else "f64",
         "data": "synthetic (SplitMix64-seeded)",
-        "config": {"workload": args.workload, "description": wl["desc"], "arith": arith_desc,
-                   "points": total, "l2": f"inputs larger than L2 ({total * es >> 20} MiB array vs "
-                                          f"129 MB L2)" if total * es > L2_BYTES else
-                   "array fits in L2 (latency-bound size)",
-                   "parallelism": f"replicas x{ws}"},
+        "config": workload_config(args, wl),
+        "arith": arith_desc,
         "hbm_gbs_effective": round((launches / args.steps) * bytes_per_launch / (ms * 1e-3) / 1e9, 1),
         "rel_l2_roundtrip": rt,
         "accuracy": accuracy,
@@ -590,7 +649,7 @@ def run_gpu(args, wl: dict) -> dict:
         "clocks": clocks,
     }
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
-        _, cpu = cpu_reference_rate(wl, budget_s=30.0, steps=1)
+        _, cpu = cpu_reference_rate(wl, budget_s=30.0, steps=5, warmup=1)
         res["cpu_baseline"] = cpu
     if dist is not None:
         dist.destroy_process_group()
@@ -706,12 +765,9 @@ def run_batch(args, wl: dict) -> dict:
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32" if f32 else "f64", "data": "synthetic (SplitMix64-seeded)",
-        "config": {"workload": args.workload, "description": wl["desc"],
-                   "transforms": len(nx), "points": total, "classes": classes,
-                   "work_items": items, "persistent_ctas": ctas,
-                   "arith": ("split " + args.split) if f32 else args.arith,
-                   "l2": f"inputs larger than L2 ({total * es >> 20} MiB vs 129 MB L2)",
-                   "parallelism": f"replicas x{ws}"},
+        "config": workload_config(args, wl),
+        "arith": ("split " + args.split) if f32 else args.arith,
+        "batch_plan": {"classes": classes, "work_items": items, "persistent_ctas": ctas},
         "mode": {0: "persistent_graph", 1: "per_class_launch_graph"}.get(auto_mode, "loop"),
         "modes_ms_per_step": {"persistent_graph": round(ms_persistent, 3),
                               "per_class_launch_graph": round(ms_launches, 3),
@@ -757,7 +813,8 @@ def cpu_batch_rate(nx, ny, budget_s=20.0):
         t += time.perf_counter() - t0
         flops += 2 * 5.0 * a * b * np.log2(a * b)
         i += 1
-    return {"value": round(flops / t / 1e9, 4), "unit": "GFLOP/s", "cores": cores, "kind": kind,
+    return {"value": round(flops / t / 1e9, 4), "unit": "GFLOP/s", "cores": cores,
+            "cpu_model": cpu_model(), "kind": kind,
             "sample": f"first {i} transforms of the batch, forward+inverse each, {t:.1f} s"}
 
 
@@ -779,29 +836,54 @@ def run_reference(args, wl: dict):
             "ms_per_step": round(cpu["ms_per_step"], 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (SplitMix64-seeded)",
-            "config": {"workload": args.workload, "description": wl["desc"],
-                       "parallelism": "host cores of rank 0"},
+            "config": workload_config(args, wl),
+            "arith": "the reference's FP64 kernels on the host cores of rank 0",
             "cpu_baseline": cpu,
             "e2e": {"value": sig(gflops), "unit": "GFLOP/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
 
 
+def companion(args, wl: dict, res64: dict, label: str, *, workload=None, arith=None,
+              split=None) -> dict:
+    """One extra measurement on the default line: the same (or a named)
+    workload with another arithmetic, with its own roofline, accuracy and
+    speed-up over the line's plain FP64 value."""
+    a = argparse.Namespace(**vars(args))
+    a.no_cpu_baseline, a.steps = True, min(args.steps, 20)
+    if workload is not None:
+        a.workload = workload
+        wl = WORKLOADS[workload]
+    if arith is not None:
+        a.arith = arith
+    if split is not None:
+        a.split = split
+        wl = dict(wl, f32=True)
+    r = run_gpu(a, wl)
+    out = {"mode": label, "workload": a.workload, "value": r["value"], "unit": r["unit"],
+           "ms_per_step": r["ms_per_step"], "steps": a.steps,
+           "rel_l2_roundtrip": r["rel_l2_roundtrip"],
+           "speedup_vs_fp64_line": round(r["value"] / res64["value"], 3),
+           "roofline": r.get("roofline"), "e2e": (r.get("e2e") or {}).get("value"),
+           "gpu_launches": r.get("gpu_launches"), "clocks": r.get("clocks")}
+    if r.get("accuracy"):
+        out["accuracy"] = r["accuracy"]
+    return out
+
+
 def split_companion(args, wl: dict, res64: dict) -> dict:
     """The metric sets the plain FP64 path against the split-precision form at
-    its stated error: the same workload with FP32 storage (accurate mode,
-    input with the 1e6 Gaussian pulse), its rel-L2 against the library's
-    FP64 path, and its speed-up over the FP64 line."""
-    a = argparse.Namespace(**vars(args))
-    a.split, a.no_cpu_baseline, a.steps = "accurate", True, min(args.steps, 20)
-    r = run_gpu(a, dict(wl, f32=True))
+    its stated error: the same workload with FP32 storage (input with the 1e6
+    Gaussian pulse), its rel-L2 against the library's FP64 path (itself
+    parity-tested against the oracle), and its speed-up over the FP64 line."""
+    r = companion(args, wl, res64, "split precision, " + args.split_companion_mode,
+                  split=args.split_companion_mode)
     acc = r.get("accuracy") or {}
-    return {"mode": "accurate (FP32 data, double-float butterflies)", "value": r["value"],
-            "unit": r["unit"], "ms_per_step": r["ms_per_step"], "steps": a.steps,
-            "rel_l2_vs_fp64": acc.get("rel_l2_vs_fp64"), "max_abs_vs_fp64": acc.get("max_abs_vs_fp64"),
-            "gate": 1e-7, "speedup_vs_fp64": round(r["value"] / res64["value"], 3),
-            "roofline_frac": (r.get("roofline") or {}).get("frac"),
-            "e2e": (r.get("e2e") or {}).get("value"),
-            "input": "the same workload's uniform field plus a 1e6 Gaussian pulse, stored as FP32"}
+    r.update({"rel_l2_vs_fp64": acc.get("rel_l2_vs_fp64"),
+              "max_abs_vs_fp64": acc.get("max_abs_vs_fp64"), "gate": 1e-7,
+              "speedup_vs_fp64": r["speedup_vs_fp64_line"],
+              "roofline_frac": (r.get("roofline") or {}).get("frac"),
+              "input": "the same workload's uniform field plus a 1e6 Gaussian pulse, stored as FP32"})
+    return r
 
 
 def main(argv=None):
@@ -817,6 +899,10 @@ def main(argv=None):
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-split-companion", action="store_true",
                     help="skip the split-precision run added to FP64 complex workloads")
+    ap.add_argument("--split-companion-mode", choices=sorted(SPLIT_MODES), default="accurate",
+                    help="split-precision mode of that run")
+    ap.add_argument("--no-companions", action="store_true",
+                    help="skip the double-float and 3D 256^3 runs added to the default line")
     args = ap.parse_args(argv)
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
@@ -832,6 +918,15 @@ def main(argv=None):
                 and not wl.get("real") and npts & (npts - 1) == 0
                 and int(os.environ.get("WORLD_SIZE", "1")) == 1):
             res["split_precision"] = split_companion(args, wl, res)
+        if (res is not None and not args.no_companions and args.workload == "1d_2p24"
+                and args.arith == "fp64" and int(os.environ.get("WORLD_SIZE", "1")) == 1):
+            # the double-float arithmetic on FP64 data (same gate as FP64)
+            # and the second workload of the FP64 target, 3D 256^3
+            res["df64"] = companion(args, wl, res, "double-float FP64 (FP32 pairs)",
+                                    arith="df64")
+            res["fp64_3d_256"] = companion(args, wl, res, "native FP64", workload="3d_256")
+            res["df64_3d_256"] = companion(args, wl, res, "double-float FP64 (FP32 pairs)",
+                                           workload="3d_256", arith="df64")
     if res is not None:
         print(json.dumps(res), flush=True)
 

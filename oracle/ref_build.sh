@@ -3,14 +3,15 @@
 # (src/kernels{1,2,3}D.cl) compiled as C++ and driven in the reference's host
 # order by oracle/ref_driver.cpp.  Test infrastructure only.
 #
-# The reference is read where it lies (TOPEFFT_REFERENCE, default
-# /root/reference); the rewritten sources and the library go to oracle/_ref/,
+# The reference is read where it lies: the directory TOPEFFT_REFERENCE names,
+# else a checkout named "reference" beside this repository; the rewritten
+# sources and the library go to oracle/_ref/,
 # which is git-ignored.  When the reference tree is absent but oracle/_ref/
 # already holds the rewritten sources (copied along with the working tree),
 # only the compile step runs.  Exit status 3 means "reference unavailable".
 set -e
 HERE=$(cd "$(dirname "$0")" && pwd)
-REF=${TOPEFFT_REFERENCE:-/root/reference}
+REF=${TOPEFFT_REFERENCE:-$HERE/../../reference}
 OUT="$HERE/_ref"
 mkdir -p "$OUT"
 if [ -d "$REF/src" ]; then

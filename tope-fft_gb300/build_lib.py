@@ -1,9 +1,10 @@
-"""Build the library (libtopefft.so) and the CPU oracle in-tree.
+"""Build the library (libtopefft.so) in-tree.
 
 libtopefft.so: the C host library (csrc/*.c, gcc) plus the CUDA kernels
 (csrc/*.cu, nvcc for sm_103a only), linked with the static CUDA runtime.
 Translation units compile in parallel; outputs go to _build/ and the
-package directory.  Nothing here needs torch.
+package directory.  Nothing here needs torch.  (The CPU oracle, test
+infrastructure, is built by oracle.build(), not here.)
 """
 from __future__ import annotations
 
