@@ -190,7 +190,7 @@ def test_c2r_nd_from_uploaded_spectrum(T, fw, orc, dims):
 
 
 # ---------------------------------------------------------------- FP32 storage
-SPLIT_GATES = {"accurate": 1e-7, "fast": 2.5e-7, "tensor": 5e-7}
+SPLIT_GATES = {"accurate": 1e-7, "fast": 2.5e-7, "tensor": 1e-7}
 SPLIT_CASES = [((4096, 1, 1), 1), ((1 << 20, 1, 1), 1), ((64, 1, 1), 33), ((1 << 14, 1, 1), 64),
                ((1000, 1, 1), 8), ((256, 128, 1), 1), ((64, 32, 16), 1), ((100, 60, 1), 1)]
 

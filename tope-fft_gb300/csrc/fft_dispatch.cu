@@ -27,8 +27,10 @@ static LaunchFn find(int log_l, int b_tile, int arith, int ept)
     if (log_l > TFFT_MAX_LOG_L_ARITH(arith)) return nullptr;
     if (arith == TFFT_ARITH_F64)
         return log_l <= 9 ? launcher_f64_lo(log_l, log_b) : launcher_f64_hi(log_l, log_b);
-    if (arith == TFFT_ARITH_F32 || (arith == TFFT_ARITH_TC && log_l < 4))
+    if (arith == TFFT_ARITH_F32)
         return log_l <= 9 ? launcher_f32_lo(log_l, log_b) : launcher_f32_hi(log_l, log_b);
+    /* lines of the tensor form below 16 points: the accurate form's kernel */
+    if (arith == TFFT_ARITH_TC) arith = TFFT_ARITH_DF32;
     if (arith == TFFT_ARITH_DF64) {
         if (log_l <= 4) return launcher_df64_0(log_l, log_b);
         if (log_l <= 6) return launcher_df64_1(log_l, log_b);

@@ -1,6 +1,7 @@
 /*
  * The tensor form of the split-precision pass (fft_tc.cuh): kernel,
- * launchers for log2 L = 4..13, the DFT-16 matrix table and the error word.
+ * launchers for log2 L = 4..13, the table of the six B matrices and the
+ * error word.
  */
 #include <cuda_runtime.h>
 
@@ -25,7 +26,7 @@ __global__ void __launch_bounds__(Cfg<LOG_L>::NT, 512 / Cfg<LOG_L>::TCOLS) tc_pa
     uint32_t *slot = reinterpret_cast<uint32_t *>(bsm + kBBytes + 8);
     const int t = threadIdx.x;
 
-    /* F's pieces (6 KB, L2-resident) into shared memory */
+    /* the six B matrices (12 KB, L2-resident) into shared memory */
     const uint4 *src = reinterpret_cast<const uint4 *>(p.mma_b);
     for (int i = t; i < kBBytes / 16; i += NT) reinterpret_cast<uint4 *>(bsm)[i] = __ldg(src + i);
     if (t < 32) {
@@ -51,8 +52,13 @@ __global__ void __launch_bounds__(Cfg<LOG_L>::NT, 512 / Cfg<LOG_L>::TCOLS) tc_pa
     line.cx.bsm = smem_u32(bsm);
     line.cx.err = &g_tc_err;
     line.cx.phase = 0;
-    run_tile<ArithF32, LOG_L, B, false, Line>(p, blockIdx.x, smem_raw, line);
+    line.cx.fail_phase = 0;
+    line.cx.dead = 0;
+    run_tile<ArithDF32, LOG_L, B, false, Line>(p, blockIdx.x, smem_raw, line);
 
+    /* after a wait that gave up: the MMAs it waited for may still be in
+     * flight; give them one more bounded wait before the columns are freed */
+    if (line.cx.dead) wait_phase(line.cx.mbar, line.cx.fail_phase);
     fence_before();
     __syncthreads();
     if (t < 32)
@@ -89,26 +95,21 @@ static const TcFn g_launch[14] = {nullptr,     nullptr,     nullptr,     nullptr
                                   &launch<5>,  &launch<6>,  &launch<7>,  &launch<8>,  &launch<9>,
                                   &launch<10>, &launch<11>, &launch<12>, &launch<13>};
 
-/* F = the real 32x32 DFT-16 (row 2k: re X_k, row 2k+1: im X_k; column 2p:
- * re x_p, column 2p+1: im x_p), rounded to FP32 and split exactly into three
- * BF16 pieces by truncation; piece i at i * 2048 bytes in b_offset layout */
+/* the six B matrices of the tensor stages (fft_tc_split.cuh b_values):
+ * F = the real 32x32 DFT-16 (row 2k: re X_k, row 2k+1: im X_k; column 2p:
+ * re x_p, column 2p+1: im x_p) from FP64 sincospi, split into integer FP16
+ * pieces and scaled; matrix m at m * 2048 bytes in b_offset layout */
 __global__ void k_tc_matrix(unsigned short *out)
 {
     for (int i = threadIdx.x; i < 32 * 32; i += blockDim.x) {
         const int n = i >> 5, k = i & 31;
-        const int kk = n >> 1, pp = k >> 1;
         double s, c;
-        sincospi((double)((kk * pp) & 15) / 8.0, &s, &c);
-        double v;
-        if ((n & 1) == 0) v = (k & 1) ? s : c; /* re X: xr cos + xi sin */
-        else v = (k & 1) ? c : -s;             /* im X: xi cos - xr sin */
-        float r = (float)v;
+        sincospi((double)(((n >> 1) * (k >> 1)) & 15) / 8.0, &s, &c);
+        double b[kNB];
+        tcs::b_values(tcs::dft16_entry(n, k, c, s), b);
 #pragma unroll
-        for (int piece = 0; piece < 3; piece++) {
-            const unsigned u = __float_as_uint(r);
-            out[piece * (kBPieceBytes / 2) + b_offset(n, k) / 2] = (unsigned short)(u >> 16);
-            r = __fsub_rn(r, __uint_as_float(u & 0xffff0000u));
-        }
+        for (int m = 0; m < kNB; m++)
+            out[m * (kBPieceBytes / 2) + b_offset(n, k) / 2] = __half_as_ushort(__double2half(b[m]));
     }
 }
 

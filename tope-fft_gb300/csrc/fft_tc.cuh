@@ -6,51 +6,61 @@
  * real product y = F x, where x holds the 32 reals of the twiddled inputs
  * (re0, im0, re1, im1, ...) and F is the real 32x32 form of the DFT-16 (row
  * 2k gives re X_k, row 2k+1 gives im X_k).  A CTA's rows go 128 at a time,
- * one row per thread, into GEMMs D[128x32] = X[128x32] * F^T:
- *   - x is split exactly into three BF16 pieces x0 + x1 + x2, each the top 8
- *     significant bits of what the previous pieces left (an FP32 significand
- *     has 24); F likewise from its FP32 rounding;
- *   - D accumulates the six products with i + j <= 2, smallest first
- *     (x2F0, x1F1, x0F2, x1F0, x0F1, x0F0), in FP32 in tensor memory; the
- *     products left out are below 2^-24 of the result;
+ * one row per thread, into GEMMs D[128x32] = X[128x32] * B^T
+ * (tcgen05.mma kind::f16, M = 128, N = 32, K = 16, FP16 in, FP32 out):
+ *   - each row is put on a fixed-point grid of its own (a power-of-two
+ *     scale from its largest value) and split into three FP16 pieces, F into
+ *     three as well (fft_tc_split.cuh); the integer leading pieces give an
+ *     exact accumulator D_hi, the five cross products a second one, D_lo:
+ *     12 MMAs per 128 rows;
  *   - the pieces of x go from registers to tensor memory (tcgen05.st, the A
- *     operand in TMEM with lane = row); F's pieces sit in shared memory in
- *     the canonical K-major layout without swizzle (the B operand, one
- *     descriptor per 16-element K half);
- *   - one thread issues the 12 MMAs (M = 128, N = 32, K = 16) of every group
- *     and commits them to an mbarrier; every thread waits for it (bounded)
- *     and reads its row of D back with tcgen05.ld.
- * The twiddles (FP64-accurate hi/lo FP32 pairs), the first stage of radix
- * 2^(log2 L mod 4), the stage exchange through shared memory and the
- * load/store path are those of the FP32 pass kernel (ArithF32).
+ *     operand in TMEM with lane = row); the six B matrices sit in shared
+ *     memory in the canonical K-major layout without swizzle (one descriptor
+ *     per 16-element K half);
+ *   - one thread issues the MMAs of every row group and commits them to an
+ *     mbarrier; every thread waits for it (bounded) and reads its row of
+ *     D_hi and D_lo back with tcgen05.ld, and renormalises their sum into
+ *     the double-float result.
+ * Everything around the GEMMs is the accurate split form's (ArithDF32):
+ * exact FP32 loads, double-float twiddles from FP64-accurate (hi, lo) tables
+ * (fused into the split), the first stage of radix 2^(log2 L mod 4) and the
+ * exchange between stages in double-float, and one rounding at the FP32
+ * store.  So the data carries about 32 bits through a pass.
  *
- * A CTA holds 2^12 points (two row groups, 256 threads, 256 TMEM columns) or,
- * for L = 2^13, 2^13 points (four groups, 512 threads, 512 columns).  Its
- * dynamic shared memory is padded so that no more CTAs share an SM than its
- * 512 TMEM columns serve.
+ * A CTA holds 2^12 points (two row groups, 256 threads, 224 of 256 TMEM
+ * columns) or, for L = 2^13, 2^13 points (four groups, 512 threads, 448 of
+ * 512 columns).  Its dynamic shared memory is at least 80 KB (116 KB) so that
+ * no more CTAs share an SM than its 512 TMEM columns serve.
+ *
+ * A wait for the tensor cores that runs out sets the device error word; the
+ * CTA then agrees on it at the next barrier, issues no further MMAs, waits
+ * (bounded) for the ones in flight and frees its tensor memory.
  */
 #pragma once
 #include <stdint.h>
 
 #include "fft_pass.cuh"
+#include "fft_tc_split.cuh"
 
 namespace tfft {
 namespace tc {
 
-constexpr int kRows = 128;                            /* rows per MMA (M)          */
-constexpr int kDCols = 32;                            /* FP32 columns of D (N)     */
-constexpr int kAPieceCols = 16;                       /* 32 BF16 K values, packed  */
-constexpr int kGroupCols = kDCols + 3 * kAPieceCols;  /* TMEM columns per group    */
-constexpr int kBPieceBytes = 2048;                    /* 32 x 32 BF16              */
-constexpr int kBBytes = 3 * kBPieceBytes;
+using tcs::kNB;
+constexpr int kRows = 128;                            /* rows per MMA (M)             */
+constexpr int kDCols = 32;                            /* FP32 columns of D (N)        */
+constexpr int kAPieceCols = 16;                       /* 32 FP16 K values, packed     */
+constexpr int kDHi = 0, kDLo = kDCols, kAOff = 2 * kDCols;
+constexpr int kGroupCols = 2 * kDCols + 3 * kAPieceCols; /* TMEM columns per group    */
+constexpr int kBPieceBytes = 2048;                    /* 32 x 32 FP16                 */
+constexpr int kBBytes = kNB * kBPieceBytes;
 constexpr int kWaitLimit = 1 << 22; /* mbarrier polls before a wait gives up */
 
 static_assert(kBBytes == TFFT_TC_MATRIX_BYTES, "matrix table size");
 
 /* shape of a CTA for log2 L: 2^12 points (2^13 for L = 2^13), one 16-point
  * row per thread, TMEM columns for all row groups, and dynamic shared
- * memory (data tile, F's pieces, mbarrier, TMEM address slot) padded so that
- * at most 512 / TCOLS CTAs fit an SM */
+ * memory (data tile, the B matrices, mbarrier, TMEM address slot) padded so
+ * that at most 512 / TCOLS CTAs fit an SM */
 template <int LOG_L>
 struct Cfg {
     static constexpr int TILE_LOG = LOG_L > 12 ? LOG_L : 12;
@@ -59,13 +69,14 @@ struct Cfg {
     static constexpr int NG = NT / kRows;
     static constexpr int TCOLS = NG * kGroupCols <= 256 ? 256 : 512;
     static constexpr size_t TILE_BYTES =
-        (pass_smem_bytes<ArithF32, LOG_L, B>() + 1023) & ~(size_t)1023;
+        (pass_smem_bytes<ArithDF32, LOG_L, B>() + 1023) & ~(size_t)1023;
     static constexpr size_t NEED = TILE_BYTES + kBBytes + 16;
     static constexpr size_t FLOOR = TCOLS == 256 ? 80 * 1024 : 116 * 1024;
     static constexpr size_t SMEM = NEED > FLOOR ? NEED : FLOOR;
+    static_assert(NG * kGroupCols <= TCOLS, "tensor memory");
 };
 
-/* byte offset of F[n][k] inside one piece: 8x8 core matrices of 16-bit
+/* byte offset of B[n][k] inside one matrix: 8x8 core matrices of 16-bit
  * values, each 8 rows (n) of 16 contiguous bytes (k); the next 8 rows lie
  * 128 B further on (SBO), the next 8 k 512 B further on (LBO) */
 __host__ __device__ constexpr int b_offset(int n, int k)
@@ -73,10 +84,10 @@ __host__ __device__ constexpr int b_offset(int n, int k)
     return (k >> 3) * 512 + (n >> 3) * 128 + (n & 7) * 16 + (k & 7) * 2;
 }
 
-/* instruction descriptor of kind::f16: D FP32, A and B BF16, both K-major,
+/* instruction descriptor of kind::f16: D FP32, A and B FP16, both K-major,
  * dense, N = 32, M = 128 */
-constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) |
-                            ((uint32_t)(kDCols >> 3) << 17) | ((uint32_t)(kRows >> 4) << 24);
+constexpr uint32_t kIdesc = (1u << 4) | ((uint32_t)(kDCols >> 3) << 17) |
+                            ((uint32_t)(kRows >> 4) << 24);
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p)
 {
@@ -100,19 +111,11 @@ __device__ __forceinline__ void fence_after()
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 }
 
-/* x = three BF16 pieces, each packed as (re, im) into one 32-bit column:
- * the low half is the even K element */
-__device__ __forceinline__ void split3(float2 v, uint32_t &p0, uint32_t &p1, uint32_t &p2)
+/* two FP32 values as one FP16 pair: the low half is the even K element */
+__device__ __forceinline__ uint32_t pack_h2(float lo, float hi)
 {
-    const uint32_t r0 = __float_as_uint(v.x), i0 = __float_as_uint(v.y);
-    p0 = __byte_perm(r0, i0, 0x7632);
-    const float r1 = __fsub_rn(v.x, __uint_as_float(r0 & 0xffff0000u));
-    const float i1 = __fsub_rn(v.y, __uint_as_float(i0 & 0xffff0000u));
-    const uint32_t ur1 = __float_as_uint(r1), ui1 = __float_as_uint(i1);
-    p1 = __byte_perm(ur1, ui1, 0x7632);
-    const float r2 = __fsub_rn(r1, __uint_as_float(ur1 & 0xffff0000u));
-    const float i2 = __fsub_rn(i1, __uint_as_float(ui1 & 0xffff0000u));
-    p2 = __byte_perm(__float_as_uint(r2), __float_as_uint(i2), 0x7632);
+    const __half2 h = __floats2half2_rn(lo, hi);
+    return *reinterpret_cast<const uint32_t *>(&h);
 }
 
 /* the three A pieces of this thread's row into its lane, columns
@@ -138,7 +141,7 @@ __device__ __forceinline__ void store_pieces(uint32_t taddr, const uint32_t (&a)
         : "memory");
 }
 
-/* this thread's row of D (32 FP32 columns), complete on return */
+/* 32 FP32 columns of this thread's lane, complete on return */
 __device__ __forceinline__ void load_row(uint32_t taddr, uint32_t (&d)[32])
 {
     asm volatile(
@@ -192,80 +195,112 @@ __device__ __forceinline__ bool wait_phase(uint32_t mbar, uint32_t parity)
 struct Ctx {
     uint32_t tm;   /* TMEM base address (lane 0, first allocated column) */
     uint32_t mbar; /* shared address of the MMA-completion mbarrier */
-    uint32_t bsm;  /* shared address of F's three pieces */
+    uint32_t bsm;  /* shared address of the six B matrices */
     int *err;      /* set to 1 when a wait gives up */
     uint32_t phase;
+    uint32_t fail_phase; /* parity of the wait that gave up */
+    int dead;            /* CTA-uniform: a wait gave up, issue no more MMAs */
 };
 
 /*
  * One radix-16 Stockham stage after NS points have been combined (the index
  * arithmetic of tfft::stage with R = 16), the DFT-16 on the tensor cores.
+ * a[] holds the thread's row in double-float on entry (FROM_SMEM false) or
+ * is read from the exchange buffer, and holds the stage's output on return.
  */
 template <int LOG_L, int B, int NS, bool FROM_SMEM, bool TO_SMEM>
-__device__ __forceinline__ void stage16(float2 *a, float2 *sm, int j, int b, const void *tw, Ctx &cx)
+__device__ __forceinline__ void stage16(ArithDF32::C *a, float4 *sm, int j, int b, const void *tw,
+                                        Ctx &cx)
 {
-    using A = ArithF32;
+    using A = ArithDF32;
     constexpr int L = 1 << LOG_L, TPL = L / 16, NT = TPL * B, NG = NT / kRows;
     static_assert(NT % kRows == 0, "whole row groups");
+    if (cx.dead) return; /* CTA-uniform */
     if constexpr (FROM_SMEM) {
 #pragma unroll
-        for (int q = 0; q < 16; q++) a[q] = sm[sidx<B>(j + q * TPL, b)];
+        for (int q = 0; q < 16; q++) a[q] = A::from_smem(sm[sidx<B>(j + q * TPL, b)]);
     }
-    if constexpr (NS > 1) {
-        const int k = j & (NS - 1);
+    /* the row's bound before the twiddle; the twiddled parts stay below
+     * sqrt2 times it (1.4375 > sqrt2 with room for rounding) */
+    float m = 0.f;
 #pragma unroll
-        for (int r = 1; r < 16; r++)
-            a[r] = A::mul_tw(a[r], A::load_tw(tw, (int64_t)(r * k) * (L / (NS * 16))));
-    }
+    for (int q = 0; q < 16; q++)
+        m = fmaxf(m, fmaxf(fabsf(a[q].r.h) + fabsf(a[q].r.l), fabsf(a[q].i.h) + fabsf(a[q].i.l)));
+    if constexpr (NS > 1) m *= 1.4375f;
+    const int sexp = tcs::scale_exp(m);
+    const float sc = tcs::pow2f(sexp);
     const int t = threadIdx.x;
     const uint32_t grp = cx.tm + (uint32_t)((t / kRows) * kGroupCols);
     const uint32_t lane = (uint32_t)(t & 96) << 16; /* this warp's 32 TMEM lanes */
     {
         uint32_t x0[16], x1[16], x2[16];
+        const int k = j & (NS - 1);
 #pragma unroll
-        for (int r = 0; r < 16; r++) split3(a[r], x0[r], x1[r], x2[r]);
-        store_pieces(grp + lane + kDCols, x0, x1, x2);
+        for (int r = 0; r < 16; r++) {
+            float pr[3], pi[3];
+            if (NS > 1 && r > 0) {
+                tcs::split_tw(a[r].r, a[r].i,
+                              A::load_tw(tw, (int64_t)(r * k) * (L / (NS * 16))), sc, pr, pi);
+            } else {
+                tcs::split_plain(a[r].r, a[r].i, sc, pr, pi);
+            }
+            x0[r] = pack_h2(pr[0], pi[0]);
+            x1[r] = pack_h2(pr[1], pi[1]);
+            x2[r] = pack_h2(pr[2], pi[2]);
+        }
+        store_pieces(grp + lane + kAOff, x0, x1, x2);
     }
     fence_before();
     __syncthreads();
     if (t == 0) {
         fence_after();
-        /* pieces (i of x, j of F), smallest products first */
-        constexpr int pi[6] = {2, 1, 0, 1, 0, 0}, pj[6] = {0, 1, 2, 0, 1, 0};
 #pragma unroll
         for (int g = 0; g < NG; g++) {
-            const uint32_t d = cx.tm + (uint32_t)(g * kGroupCols);
+            const uint32_t base = cx.tm + (uint32_t)(g * kGroupCols);
 #pragma unroll
-            for (int s = 0; s < 6; s++)
+            for (int q = 0; q < kNB; q++)
 #pragma unroll
                 for (int h = 0; h < 2; h++)
-                    mma(d, d + kDCols + pi[s] * kAPieceCols + 8 * h,
-                        b_desc(cx.bsm + pj[s] * kBPieceBytes + h * 1024), (s | h) != 0);
+                    mma(base + (q == 0 ? kDHi : kDLo),
+                        base + kAOff + tcs::prod_a(q) * kAPieceCols + 8 * h,
+                        b_desc(cx.bsm + tcs::prod_b(q) * kBPieceBytes + h * 1024),
+                        (q >= 2 || h) ? 1u : 0u);
         }
         commit(cx.mbar);
     }
     const bool ok = wait_phase(cx.mbar, cx.phase);
+    if (!ok) cx.fail_phase = cx.phase;
     cx.phase ^= 1;
-    if (!ok) atomicExch(cx.err, 1);
     fence_after();
     {
-        uint32_t d[32];
-        load_row(grp + lane, d);
+        uint32_t dh[32], dl[32];
+        load_row(grp + lane + kDHi, dh);
+        load_row(grp + lane + kDLo, dl);
+        const float sh = tcs::pow2f(-sexp - tcs::kFB);
+        const float sl = tcs::pow2f(-sexp - tcs::kFB - tcs::kLoShift);
 #pragma unroll
-        for (int r = 0; r < 16; r++) a[r] = make_float2(__uint_as_float(d[2 * r]), __uint_as_float(d[2 * r + 1]));
+        for (int r = 0; r < 16; r++) {
+            a[r].r = tcs::join_d(__uint_as_float(dh[2 * r]), __uint_as_float(dl[2 * r]), sh, sl);
+            a[r].i = tcs::join_d(__uint_as_float(dh[2 * r + 1]), __uint_as_float(dl[2 * r + 1]), sh, sl);
+        }
     }
     if constexpr (TO_SMEM) {
         const int k = j & (NS - 1);
         const int o = (j / NS) * NS * 16 + k;
 #pragma unroll
-        for (int r = 0; r < 16; r++) sm[sidx<B>(o + r * NS, b)] = a[r];
-        __syncthreads();
+        for (int r = 0; r < 16; r++) sm[sidx<B>(o + r * NS, b)] = A::to_smem(a[r]);
+    }
+    /* the exchange barrier, which also makes a give-up CTA-uniform */
+    if (__syncthreads_or(!ok)) {
+        cx.dead = 1;
+        if (t == 0) atomicExch(cx.err, 1);
     }
 }
 
 /* radix-16 stages S .. NSTAGE-1 */
 template <int LOG_L, int B, int S>
-__device__ __forceinline__ void stages(float2 *a, float2 *sm, int j, int b, const void *tw, Ctx &cx)
+__device__ __forceinline__ void stages(ArithDF32::C *a, float4 *sm, int j, int b, const void *tw,
+                                       Ctx &cx)
 {
     using SH = Shape<LOG_L>;
     if constexpr (S < SH::NSTAGE) {
@@ -281,13 +316,16 @@ __device__ __forceinline__ void stages(float2 *a, float2 *sm, int j, int b, cons
 struct Line {
     Ctx cx;
     template <class A, int LOG_L, int B, int EPT = 16>
-    __device__ __forceinline__ void run(float2 *a, float2 *sm, int j, int b, const tfft_pass &p)
+    __device__ __forceinline__ void run(typename A::C *a, typename A::S *sm, int j, int b,
+                                        const tfft_pass &p)
     {
         static_assert(EPT == 16, "the tensor stages hold 16 points per thread");
         static_assert(LOG_L >= 4, "a radix-16 stage needs 16 points");
+        static_assert(sizeof(typename A::S) == sizeof(float4), "double-float exchange");
         using SH = Shape<LOG_L>;
         if constexpr (SH::LR0) {
-            stage<ArithF32, LOG_L, B, SH::R0, 1, false, true>(a, sm, j, b, p.tw);
+            /* first stage of radix 2, 4 or 8 on the CUDA cores, double-float */
+            stage<ArithDF32, LOG_L, B, SH::R0, 1, false, true>(a, sm, j, b, p.tw);
         } else {
             stage16<LOG_L, B, 1, false, (SH::NSTAGE > 1)>(a, sm, j, b, p.tw, cx);
         }

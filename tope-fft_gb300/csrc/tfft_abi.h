@@ -23,8 +23,9 @@ enum tfft_arith {
                             float butterflies on chip, so only the FP32 loads
                             and stores round                                  */
     TFFT_ARITH_TC = 4,   /* split precision, tensor: FP32 storage, radix-16
-                            stages as tcgen05 GEMMs on 3-way BF16 splits with
-                            FP32 accumulation; other stages as TFFT_ARITH_F32 */
+                            stages as tcgen05 GEMMs on 3-piece FP16 splits
+                            (an exact and a cross-product FP32 accumulator);
+                            everything else as TFFT_ARITH_DF32              */
 };
 
 /* bytes of one complex element in memory for an arithmetic */
@@ -75,8 +76,8 @@ typedef struct tfft_pass {
      * replaces g1*is[1] (and g1*os[1]); used by batches of transforms that
      * sit at arbitrary offsets of the caller's packed buffer */
     const int64_t *tab0, *tab1;
-    /* TFFT_ARITH_TC: the 3 BF16 pieces of the real 32x32 DFT-16 matrix in
-     * the tensor cores' shared-memory layout (tfft_tc_matrix) */
+    /* TFFT_ARITH_TC: the six FP16 B matrices (pieces of the real 32x32
+     * DFT-16) in the tensor cores' shared-memory layout (tfft_tc_matrix) */
     const void *mma_b;
     /* points per thread: 0 or 16 (radix-16 stages), or 4 (radix-4 stages,
      * FP64 storage, log2 L = 2..7: small transforms) */
@@ -176,8 +177,8 @@ int tfft_dft_table(void *tw, int n, void *stream);
 int tfft_table_any(void *tw, int len, int arith, void *stream);
 
 /* ---- tensor-core form ------------------------------------------------------ */
-/* bytes of the DFT-16 matrix table */
-#define TFFT_TC_MATRIX_BYTES 6144
+/* bytes of the table of the six B matrices */
+#define TFFT_TC_MATRIX_BYTES 12288
 int tfft_tc_matrix(void *dst, void *stream);
 /* lines per CTA the tensor form needs for log2 L (its CTAs hold 2^12 points,
  * 2^13 for L = 2^13) */
