@@ -143,6 +143,78 @@ def test_batch_autotune_cache_written_and_reused(T, fw, orc, tune_cache):
     T.topeBatchDestroy(fw, b2)
 
 
+def config5_shapes():
+    """The uneven-batch benchmark configuration, drawn as bench.py draws it:
+    20,000 1D transforms of 2^k points, k uniform on 6..16, then 500 2D
+    transforms with sides drawn independently from {64, ..., 1024}."""
+    if str(ROOT) not in sys.path:
+        sys.path.insert(0, str(ROOT))
+    import bench
+    return bench.uneven_shapes()
+
+
+def config5_sample(nx, ny, count=500, seed=SEED0 + 55):
+    """At least `count` transform indices: the first transform of every
+    shape class (all eleven 1D lengths and every 2D class, those with a 1024
+    side among them), then a seeded draw of the rest."""
+    first = {}
+    for i, shape in enumerate(zip(nx, ny)):
+        first.setdefault(shape, i)
+    idx = set(first.values())
+    for i in np.random.default_rng(seed).permutation(len(nx)):
+        if len(idx) >= count:
+            break
+        idx.add(int(i))
+    return sorted(idx)
+
+
+@pytest.mark.parametrize("arith", ["fp64", "split_accurate"])
+def test_batch_full_size_configuration(T, orc, tune_cache, arith):
+    """The whole benchmark batch (20,500 transforms, 322 M points) in one plan,
+    in the persistent structure and in the per-class launch graph; a seeded
+    sample of at least 500 transforms, one of every shape class among them,
+    against the oracle (FP64 gate, or 1e-7 for FP32 data against the oracle
+    of the unrounded input)."""
+    nx, ny = config5_shapes()
+    assert len(nx) == 20500 and max(nx) == 1 << 16
+    assert {(a, b) for a, b in zip(nx, ny) if b > 1 and 1024 in (a, b)}
+    offs = np.concatenate([[0], np.cumsum([2 * a * b for a, b in zip(nx, ny)])]).astype(np.int64)
+    x = orc.uniform(int(offs[-1]) // 2, SEED0 + 6)
+    sample = config5_sample(nx, ny)
+    assert len(sample) >= 500
+    f = T.TopeFFT()
+    T.topeFFTInit(f)
+    T.check(f)
+    if arith == "fp64":
+        T.topeSetArith(f, T.TOPE_ARITH_FP64)
+        data = x
+    else:
+        T.topeSetSplitMode(f, 0)
+        data = x.astype(np.float32)
+    b = T.TopeBatch()
+    T.topeBatchPlanInit(f, b, nx, ny, T.C2C, data)
+    T.check(f)
+    refs = {i: orc.exec(x[offs[i]:offs[i + 1]], nx[i], ny[i], 1, 1) for i in sample}
+    got = np.empty_like(data)
+    for mode in ("persistent", "launches"):
+        T.topeBatchSetMode(f, b, MODES[mode])
+        T.check(f)
+        got[:] = np.nan
+        T.topeBatchUpload(f, b, data)
+        T.topeBatchExec(f, b, got, T.FORWARD)
+        T.check(f)
+        bad = []
+        for i in sample:
+            n = nx[i] * ny[i]
+            err = orc.rel_l2(got[offs[i]:offs[i + 1]].astype(np.float64), refs[i])
+            gate = tol_fp64(n) if arith == "fp64" else 1e-7
+            if not err <= gate:
+                bad.append((mode, nx[i], ny[i], err))
+        assert not bad, bad[:5]
+    T.topeBatchDestroy(f, b)
+    T.topeFFTDestroy(f)
+
+
 def test_batch_rejects_bad_sizes(T, fw):
     b = T.TopeBatch()
     T.topeBatchPlanInit(fw, b, [64, 48], [1, 1], T.C2C, np.zeros(2 * 112))
