@@ -4,11 +4,13 @@
 // with _Float16; D_hi summed exactly in double and required to be an integer
 // below 2^24, so that FP32 accumulation in any order is exact; D_lo summed in
 // FP32 in K order).  Single rows are checked against a long-double DFT-16 of
-// the same (twiddled) rows; whole lines of 256, 512 and 4096 points run the
+// the same (twiddled) rows; whole lines of 2^8 .. 2^12 points run the
 // kernel's Stockham stages (index arithmetic of fft_tc.cuh stage16, its
-// first stage of radix 2^(log2 L mod 4) here in long double) and are checked
-// against a long-double DFT.  Prints one line per check; exit status 0 when
-// all pass.
+// first stage of radix 2^(log2 L mod 4) through the pass code's double-float
+// butterflies, and the renormalising read after it) and are checked against
+// a long-double DFT, for uniform data, a 1e6 pulse and a pure tone (whose
+// first-stage sums cancel exactly).  Prints one line per check; exit status
+// 0 when all pass.
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -16,6 +18,7 @@
 #include <vector>
 
 #include "cuda_runtime.h"
+#include "fft_pass.cuh"
 #include "fft_tc_split.cuh"
 
 using namespace tfft;
@@ -64,13 +67,19 @@ struct dfc {
 
 /* one radix-16 stage of a line of L points after NS points were combined:
  * the kernel's stage16 on the host */
-static void tc_line_stage(std::vector<dfc> &a, int L, int NS, const std::vector<float4> &tw)
+static void tc_line_stage(std::vector<dfc> &a, int L, int NS, const std::vector<float4> &tw,
+                          bool renorm)
 {
     const int TPL = L / 16;
     std::vector<dfc> out(L);
     for (int j = 0; j < TPL; j++) {
         dfc v[16];
         for (int q = 0; q < 16; q++) v[q] = a[j + q * TPL];
+        if (renorm)
+            for (int q = 0; q < 16; q++) {
+                two_sum(v[q].r.h, v[q].r.l, v[q].r.h, v[q].r.l);
+                two_sum(v[q].i.h, v[q].i.l, v[q].i.h, v[q].i.l);
+            }
         float m = 0;
         for (int q = 0; q < 16; q++)
             m = std::fmax(m, std::fmax(std::fabs(v[q].r.h) + std::fabs(v[q].r.l),
@@ -120,30 +129,36 @@ static double tc_line(int lg, int kind)
         xr[p] = (float)urand();
         xi[p] = (float)urand();
         if (kind == 1) xr[p] += (float)(1e6 * std::exp(-0.5 * (p - L / 2) * (p - L / 2) / 16.0));
+        if (kind == 2) { /* a tone: its first-stage sums cancel exactly */
+            const long double ang = 2 * PI * (long double)((p * 37) % L) / L;
+            xr[p] = (float)cosl(ang);
+            xi[p] = (float)sinl(ang);
+        }
     }
     std::vector<dfc> a(L);
     for (int p = 0; p < L; p++) a[p] = dfc{df2{xr[p], 0.f}, df2{xi[p], 0.f}};
     const int lr0 = lg % 4;
     int ns = 1;
     if (lr0) {
+        /* the kernel's first stage: the double-float butterflies of the
+         * CUDA-core pass code (fft_pass.cuh), which leave sums unnormalised */
         const int R = 1 << lr0, m = L / R;
         std::vector<dfc> out(L);
-        for (int j = 0; j < m; j++)
-            for (int kk = 0; kk < R; kk++) {
-                long double sr = 0, si = 0;
-                for (int q = 0; q < R; q++) {
-                    const long double c = cosl(2 * PI * q * kk / R), s = -sinl(2 * PI * q * kk / R);
-                    const long double vr = (long double)a[j + q * m].r.h, vi = (long double)a[j + q * m].i.h;
-                    sr += vr * c - vi * s;
-                    si += vr * s + vi * c;
-                }
-                const float hr = (float)sr, hi = (float)si;
-                out[j * R + kk] = dfc{df2{hr, (float)(sr - hr)}, df2{hi, (float)(si - hi)}};
+        for (int j = 0; j < m; j++) {
+            ArithDF32::C c[8];
+            for (int q = 0; q < R; q++) {
+                c[q].r = a[j + q * m].r;
+                c[q].i = a[j + q * m].i;
             }
+            if (R == 2) dft<ArithDF32, 2>(c);
+            else if (R == 4) dft<ArithDF32, 4>(c);
+            else dft<ArithDF32, 8>(c);
+            for (int kk = 0; kk < R; kk++) out[j * R + kk] = dfc{c[kk].r, c[kk].i};
+        }
         a.swap(out);
         ns = R;
     }
-    for (; ns < L; ns *= 16) tc_line_stage(a, L, ns, tw);
+    for (bool first = true; ns < L; ns *= 16, first = false) tc_line_stage(a, L, ns, tw, first && lr0);
     long double e2 = 0, r2 = 0;
     for (int k = 0; k < L; k++) {
         long double sr = 0, si = 0;
@@ -298,14 +313,15 @@ int main()
     check(dhi_int, "D_hi an integer sum below 2^24 (exact in FP32)", max_dhi);
     check(worst < 2e-9, "worst row rel-L2, no twiddle", worst);
     check(worst_tw < 2e-9, "worst row rel-L2, twiddled", worst_tw);
-    /* whole lines: two (256), radix 2 + two (512) and three (4096) tensor
-     * stages, uniform and with a 1e6 pulse */
-    const int lgs[3] = {8, 9, 12};
-    for (int li = 0; li < 3; li++)
-        for (int kind = 0; kind < 2; kind++) {
+    /* whole lines: two tensor stages after a first stage of radix 1, 2, 4
+     * or 8 (256 .. 2048 points) and three (4096), uniform, with a 1e6 pulse
+     * and a pure tone */
+    const int lgs[5] = {8, 9, 10, 11, 12};
+    for (int li = 0; li < 5; li++)
+        for (int kind = 0; kind < 3; kind++) {
             char what[96];
             std::snprintf(what, sizeof what, "line 2^%d %s: rel-L2 before the FP32 store",
-                          lgs[li], kind ? "with 1e6 pulse" : "uniform");
+                          lgs[li], kind == 2 ? "one tone" : kind ? "with 1e6 pulse" : "uniform");
             const double e = tc_line(lgs[li], kind);
             check(e < 1e-8, what, e);
         }

@@ -125,8 +125,8 @@ def test_f32_round_trip_and_type_checks(T, fw, orc):
     T.check(fw)
 
 
-@pytest.mark.parametrize("lg,batch", [(4, 256), (4, 3), (5, 100), (8, 16), (9, 5), (12, 1),
-                                      (12, 3), (13, 2), (14, 2), (2, 8)])
+@pytest.mark.parametrize("lg,batch", [(4, 256), (4, 3), (5, 100), (8, 16), (9, 5), (10, 4),
+                                      (11, 2), (12, 1), (12, 3), (13, 2), (14, 2), (2, 8)])
 def test_tensor_mode_shapes(T, orc, lg, batch):
     """Every line length of the tensor form (one row group per 128 16-point
     sub-transforms, ragged last tiles, the four-step split above 2^13, the
@@ -143,6 +143,31 @@ def test_tensor_mode_shapes(T, orc, lg, batch):
         ref = orc.exec(x32.astype(np.float64), n, 1, 1, dir_, batch=batch)
         err = orc.rel_l2(got, ref)
         print(f"tensor L=2^{lg} x{batch} dir={dir_}: rel-L2 {err:.2e}")
+        assert err <= 1e-7
+    T.topeFFTDestroy(f)
+
+
+@pytest.mark.parametrize("lg", [5, 6, 7, 9, 10, 11, 12, 13])
+def test_tensor_mode_pure_tones(T, orc, lg):
+    """Lines holding one tone each: the first stage's double-float sums
+    cancel exactly in many rows, leaving values whose low part is the whole
+    value; the tensor stages must renormalise them before splitting.  Every
+    line length with a first stage of radix 2, 4 or 8 on the CUDA cores,
+    against the FP64 oracle."""
+    f = T.TopeFFT()
+    T.topeFFTInit(f)
+    T.topeSetSplitMode(f, T.TOPE_SPLIT_TENSOR)
+    T.check(f)
+    n, batch = 1 << lg, 4
+    j = np.arange(n)
+    x = np.concatenate([np.exp(2j * np.pi * ((j * (3 + 7 * b)) % n) / n) for b in range(batch)])
+    x32 = x.astype(np.complex64).view(np.float32)
+    for dir_ in (1, 0):
+        got = run_f32(T, f, x32, (n, 1, 1), dir_, batch).astype(np.float64)
+        assert np.all(np.isfinite(got))
+        ref = orc.exec(x32.astype(np.float64), n, 1, 1, dir_, batch=batch)
+        err = orc.rel_l2(got, ref)
+        print(f"tensor tones L=2^{lg} dir={dir_}: rel-L2 {err:.2e}")
         assert err <= 1e-7
     T.topeFFTDestroy(f)
 

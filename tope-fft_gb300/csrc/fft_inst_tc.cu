@@ -22,8 +22,9 @@ __global__ void __launch_bounds__(Cfg<LOG_L>::NT, 512 / Cfg<LOG_L>::TCOLS) tc_pa
     static_assert(Shape<LOG_L>::TPL * B == NT, "one row per thread");
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char *bsm = smem_raw + Cfg<LOG_L>::TILE_BYTES;
-    uint64_t *mbar = reinterpret_cast<uint64_t *>(bsm + kBBytes);
-    uint32_t *slot = reinterpret_cast<uint32_t *>(bsm + kBBytes + 8);
+    constexpr int NG = Cfg<LOG_L>::NG;
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(bsm + kBBytes); /* one per row group */
+    uint32_t *slot = reinterpret_cast<uint32_t *>(bsm + kBBytes + 8 * NG);
     const int t = threadIdx.x;
 
     /* the six B matrices (12 KB, L2-resident) into shared memory */
@@ -37,7 +38,9 @@ __global__ void __launch_bounds__(Cfg<LOG_L>::NT, 512 / Cfg<LOG_L>::TCOLS) tc_pa
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
     if (t == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(mbar)), "r"(1) : "memory");
+        for (int g = 0; g < NG; g++)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(mbar + g)), "r"(1)
+                         : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     /* F as written by these threads becomes visible to the tensor cores */
@@ -57,8 +60,10 @@ __global__ void __launch_bounds__(Cfg<LOG_L>::NT, 512 / Cfg<LOG_L>::TCOLS) tc_pa
     run_tile<ArithDF32, LOG_L, B, false, Line>(p, blockIdx.x, smem_raw, line);
 
     /* after a wait that gave up: the MMAs it waited for may still be in
-     * flight; give them one more bounded wait before the columns are freed */
-    if (line.cx.dead) wait_phase(line.cx.mbar, line.cx.fail_phase);
+     * flight in any group; give each group's one more bounded wait before
+     * the columns are freed */
+    if (line.cx.dead)
+        for (int g = 0; g < NG; g++) wait_phase(line.cx.mbar + 8u * (uint32_t)g, line.cx.fail_phase);
     fence_before();
     __syncthreads();
     if (t < 32)

@@ -34,7 +34,7 @@
  *
  * A wait for the tensor cores that runs out sets the device error word; the
  * CTA then agrees on it at the next barrier, issues no further MMAs, waits
- * (bounded) for the ones in flight and frees its tensor memory.
+ * (bounded) for every group's MMAs in flight and frees its tensor memory.
  */
 #pragma once
 #include <stdint.h>
@@ -70,7 +70,7 @@ struct Cfg {
     static constexpr int TCOLS = NG * kGroupCols <= 256 ? 256 : 512;
     static constexpr size_t TILE_BYTES =
         (pass_smem_bytes<ArithDF32, LOG_L, B>() + 1023) & ~(size_t)1023;
-    static constexpr size_t NEED = TILE_BYTES + kBBytes + 16;
+    static constexpr size_t NEED = TILE_BYTES + kBBytes + 8 * NG + 8;
     static constexpr size_t FLOOR = TCOLS == 256 ? 80 * 1024 : 116 * 1024;
     static constexpr size_t SMEM = NEED > FLOOR ? NEED : FLOOR;
     static_assert(NG * kGroupCols <= TCOLS, "tensor memory");
@@ -194,7 +194,8 @@ __device__ __forceinline__ bool wait_phase(uint32_t mbar, uint32_t parity)
 /* the per-CTA state of the tensor stages */
 struct Ctx {
     uint32_t tm;   /* TMEM base address (lane 0, first allocated column) */
-    uint32_t mbar; /* shared address of the MMA-completion mbarrier */
+    uint32_t mbar; /* shared address of row group 0's MMA-completion
+                      mbarrier; group g's lies 8 g bytes further on */
     uint32_t bsm;  /* shared address of the six B matrices */
     int *err;      /* set to 1 when a wait gives up */
     uint32_t phase;
@@ -207,18 +208,29 @@ struct Ctx {
  * arithmetic of tfft::stage with R = 16), the DFT-16 on the tensor cores.
  * a[] holds the thread's row in double-float on entry (FROM_SMEM false) or
  * is read from the exchange buffer, and holds the stage's output on return.
+ * RENORM: the row was written by a first stage on the CUDA cores, whose
+ * double-float sums are unnormalised (where high parts cancel exactly, a
+ * low part is the whole value); each part is renormalised with a two-sum,
+ * since the split needs low parts below an ulp of the high parts.
  */
-template <int LOG_L, int B, int NS, bool FROM_SMEM, bool TO_SMEM>
+template <int LOG_L, int B, int NS, bool FROM_SMEM, bool TO_SMEM, bool RENORM = false>
 __device__ __forceinline__ void stage16(ArithDF32::C *a, float4 *sm, int j, int b, const void *tw,
                                         Ctx &cx)
 {
     using A = ArithDF32;
-    constexpr int L = 1 << LOG_L, TPL = L / 16, NT = TPL * B, NG = NT / kRows;
+    constexpr int L = 1 << LOG_L, TPL = L / 16, NT = TPL * B;
     static_assert(NT % kRows == 0, "whole row groups");
     if (cx.dead) return; /* CTA-uniform */
     if constexpr (FROM_SMEM) {
 #pragma unroll
         for (int q = 0; q < 16; q++) a[q] = A::from_smem(sm[sidx<B>(j + q * TPL, b)]);
+    }
+    if constexpr (RENORM) {
+#pragma unroll
+        for (int q = 0; q < 16; q++) {
+            two_sum(a[q].r.h, a[q].r.l, a[q].r.h, a[q].r.l);
+            two_sum(a[q].i.h, a[q].i.l, a[q].i.h, a[q].i.l);
+        }
     }
     /* the row's bound before the twiddle; the twiddled parts stay below
      * sqrt2 times it (1.4375 > sqrt2 with room for rounding) */
@@ -251,25 +263,26 @@ __device__ __forceinline__ void stage16(ArithDF32::C *a, float4 *sm, int j, int 
         store_pieces(grp + lane + kAOff, x0, x1, x2);
     }
     fence_before();
-    __syncthreads();
-    if (t == 0) {
+    /* each row group (4 warps, 128 threads) on its own: a named barrier,
+     * then one thread issues the group's MMAs and commits them to the
+     * group's mbarrier, so one group's MMAs overlap the other's split */
+    const int g = t / kRows;
+    asm volatile("bar.sync %0, %1;" ::"r"(1 + g), "r"(kRows) : "memory");
+    const uint32_t gmbar = cx.mbar + 8u * (uint32_t)g;
+    if ((t & (kRows - 1)) == 0) {
         fence_after();
+        const uint32_t base = cx.tm + (uint32_t)(g * kGroupCols);
 #pragma unroll
-        for (int g = 0; g < NG; g++) {
-            const uint32_t base = cx.tm + (uint32_t)(g * kGroupCols);
+        for (int q = 0; q < kNB; q++)
 #pragma unroll
-            for (int q = 0; q < kNB; q++)
-#pragma unroll
-                for (int h = 0; h < 2; h++)
-                    mma(base + (q == 0 ? kDHi : kDLo),
-                        base + kAOff + tcs::prod_a(q) * kAPieceCols + 8 * h,
-                        b_desc(cx.bsm + tcs::prod_b(q) * kBPieceBytes + h * 1024),
-                        (q >= 2 || h) ? 1u : 0u);
-        }
-        commit(cx.mbar);
+            for (int h = 0; h < 2; h++)
+                mma(base + (q == 0 ? kDHi : kDLo), base + kAOff + tcs::prod_a(q) * kAPieceCols + 8 * h,
+                    b_desc(cx.bsm + tcs::prod_b(q) * kBPieceBytes + h * 1024),
+                    (q >= 2 || h) ? 1u : 0u);
+        commit(gmbar);
     }
-    const bool ok = wait_phase(cx.mbar, cx.phase);
-    if (!ok) cx.fail_phase = cx.phase;
+    const uint32_t this_phase = cx.phase;
+    const bool ok = wait_phase(gmbar, this_phase);
     cx.phase ^= 1;
     fence_after();
     {
@@ -293,6 +306,7 @@ __device__ __forceinline__ void stage16(ArithDF32::C *a, float4 *sm, int j, int 
     /* the exchange barrier, which also makes a give-up CTA-uniform */
     if (__syncthreads_or(!ok)) {
         cx.dead = 1;
+        cx.fail_phase = this_phase;
         if (t == 0) atomicExch(cx.err, 1);
     }
 }
@@ -307,7 +321,9 @@ __device__ __forceinline__ void stages(ArithDF32::C *a, float4 *sm, int j, int b
         constexpr int first_log = SH::LR0 ? SH::LR0 : 4;
         constexpr int NS = 1 << (first_log + 4 * (S - 1));
         constexpr bool last = (S == SH::NSTAGE - 1);
-        stage16<LOG_L, B, NS, true, !last>(a, sm, j, b, tw, cx);
+        /* the first tensor stage after a first stage on the CUDA cores
+         * renormalises its row */
+        stage16<LOG_L, B, NS, true, !last, (S == 1 && SH::LR0 != 0)>(a, sm, j, b, tw, cx);
         stages<LOG_L, B, S + 1>(a, sm, j, b, tw, cx);
     }
 }

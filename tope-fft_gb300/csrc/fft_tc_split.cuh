@@ -62,13 +62,12 @@ __host__ __device__ constexpr int prod_b(int q)
     return q == 0 ? 0 : q == 1 ? 4 : q == 2 ? 3 : q == 3 ? 5 : q == 4 ? 1 : 2;
 }
 
+/* v rounded to the nearest integer (ties to even) for |v| < 2^22, with two
+ * FP32 additions: v + 1.5 * 2^23 lies in (2^23, 2^24), where the ulp is 1,
+ * and the subtraction is exact (the FMA pipe, not the conversion unit) */
 __host__ __device__ __forceinline__ float rint_(float v)
 {
-#ifdef __CUDA_ARCH__
-    return rintf(v);
-#else
-    return __builtin_rintf(v);
-#endif
+    return sub_rn(add_rn(v, 12582912.f), 12582912.f);
 }
 
 __host__ __device__ __forceinline__ double rint_d(double v)
@@ -95,7 +94,7 @@ __host__ __device__ __forceinline__ int scale_exp(float m)
     return sexp < -126 ? -126 : (sexp > 126 ? 126 : sexp);
 }
 
-/* pieces of t0 + t1 + t2 (already on the row's grid, |t0| + |t1| < 2^9,
+/* pieces of t0 + t1 + t2 (already on the row's grid, |t0| + |t1| <= 2^9,
  * |t2| below 2^-13: the row's values are normalised double-floats):
  * x0 + 2^-11 x1 + 2^-22 x2, with x0, x1 integers and x2 the rest (rounded
  * to FP16 when packed).  t0 - rint(t0) and t1 - rint(t1) are exact, the
