@@ -66,6 +66,14 @@ WORKLOADS = {
                          "desc": "split precision: 1D C2C batched 4096 x 2^14, FP32 data, "
                                  "uniform field + Gaussian pulse 1e6 (sigma 4) per row, "
                                  "forward+inverse"},
+    "r2c_f32_1d_2p24": {"dims": (1 << 24, 1, 1), "batch": 1, "real": True, "f32": True,
+                        "desc": "1D real-to-complex, split precision (FP32 data), N=2^24 "
+                                "uniform[-1,1) reals, forward (R2C) + inverse (C2R); GFLOP/s "
+                                "counts 2.5 N log2 N per direction"},
+    "1d_97x2p20": {"dims": (97, 1, 1), "batch": 1 << 20,
+                   "desc": "1D C2C FP64, batched 2^20 x 97 (a prime below 128: the exact "
+                           "O(N^2) DFT kernel), forward+inverse, uniform[-1,1) re/im; GFLOP/s "
+                           "counts the nominal 5 N log2 N per direction"},
     "r2c_1d_2p24": {"dims": (1 << 24, 1, 1), "batch": 1, "real": True,
                     "desc": "1D real-to-complex FP64, N=2^24 uniform[-1,1) reals, forward (R2C) "
                             "+ inverse (C2R); GFLOP/s counts 2.5 N log2 N per direction"},
@@ -455,7 +463,7 @@ def run_gpu(args, wl: dict) -> dict:
         if ny * nz == 1:
             p = T.TopePlan1D()
             if single:
-                T.tope1DBatchPlanInitF32(f, p, nx, batch, T.C2C, data)
+                T.tope1DBatchPlanInitF32(f, p, nx, batch, T.R2C if real else T.C2C, data)
             elif batch == 1:
                 T.tope1DPlanInit(f, p, nx, T.R2C if real else T.C2C, data)
             else:
@@ -918,6 +926,10 @@ def main(argv=None):
                 and not wl.get("real") and npts & (npts - 1) == 0
                 and int(os.environ.get("WORLD_SIZE", "1")) == 1):
             res["split_precision"] = split_companion(args, wl, res)
+            if args.split_companion_mode != "tensor":
+                # the tensor form (tcgen05 stages) on the same workload
+                res["split_precision_tensor"] = split_companion(
+                    argparse.Namespace(**dict(vars(args), split_companion_mode="tensor")), wl, res)
         if (res is not None and not args.no_companions and args.workload == "1d_2p24"
                 and args.arith == "fp64" and int(os.environ.get("WORLD_SIZE", "1")) == 1):
             # the double-float arithmetic on FP64 data (same gate as FP64)
