@@ -572,8 +572,9 @@ def run_gpu(args, wl: dict) -> dict:
         roof = {"bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(ach / peak, 4), "peak_source": peak_kind,
                 "traffic": ncu_traffic(args.workload, SPLIT_ARITH[args.split] if f32 else args.arith),
-                "kernel": (f"pass_kernel L=2^{dom['log_l']}" if dom["log_l"] >= 0 else
-                           f"mixed_kernel L={dom['len']}") +
+                "kernel": ((f"tc_pass_kernel L=2^{dom['log_l']}" if f32 and args.split == "tensor"
+                            and dom["log_l"] >= 4 else f"pass_kernel L=2^{dom['log_l']}")
+                           if dom["log_l"] >= 0 else f"mixed_kernel L={dom['len']}") +
                           f" B={dom['b_tile']} ({dom['ctas']} CTAs x {dom['threads']} threads)",
                 "launch_us": round(avg_ns / 1e3, 2),
                 "bytes_per_launch": bytes_per_launch,

@@ -23,6 +23,7 @@
  * the inverse scale are fused into the store as in the power-of-two pass.
  */
 #pragma once
+#include <type_traits>
 #include "fft_pass.cuh"
 
 namespace tfft {
@@ -221,22 +222,29 @@ __global__ void __launch_bounds__(kMixedThreads, pass_min_blocks<A, kMixedThread
     Store *out = reinterpret_cast<Store *>(p.out);
     const bool rows_out = p.oes == 1;
     const int64_t mask = (int64_t(1) << p.tw_shift) - 1;
-    for (int idx = threadIdx.x; idx < pts; idx += kMixedThreads) {
-        const int b = rows_out ? idx / L : idx & (B - 1);
-        const int i = rows_out ? idx - b * L : idx / B;
-        const int64_t g0 = g0first + b;
-        if (g0 >= p.n[0]) continue;
-        C v = A::from_smem(res[mixed_pad(i * B + b)]);
-        if (p.post_tw) {
-            const int64_t t = p.tw_level == 0 ? g0 : g1;
-            const int64_t m = t * (int64_t)i; /* < N: no reduction needed */
-            v = A::mul_tw(v, p.tw_lo ? A::tw_mul(A::load_tw(p.tw_hi, m >> p.tw_shift),
-                                                 A::load_tw(p.tw_lo, m & mask))
-                                     : A::load_tw(p.tw_hi, m));
+    /* scale 1 (every pass but an inverse's last) in a loop of its own, so
+     * the per-element test of the double-precision scale folds away */
+    auto store_all = [&](auto unit_scale) {
+        const double scale = decltype(unit_scale)::value ? 1.0 : p.scale;
+        for (int idx = threadIdx.x; idx < pts; idx += kMixedThreads) {
+            const int b = rows_out ? idx / L : idx & (B - 1);
+            const int i = rows_out ? idx - b * L : idx / B;
+            const int64_t g0 = g0first + b;
+            if (g0 >= p.n[0]) continue;
+            C v = A::from_smem(res[mixed_pad(i * B + b)]);
+            if (p.post_tw) {
+                const int64_t t = p.tw_level == 0 ? g0 : g1;
+                const int64_t m = t * (int64_t)i; /* < N: no reduction needed */
+                v = A::mul_tw(v, p.tw_lo ? A::tw_mul(A::load_tw(p.tw_hi, m >> p.tw_shift),
+                                                     A::load_tw(p.tw_lo, m & mask))
+                                         : A::load_tw(p.tw_hi, m));
+            }
+            if (p.conj_out) v = A::conj(v);
+            __stcs(out + obase + g0 * p.os[0] + (int64_t)i * p.oes, A::store_s(v, delta_out, scale));
         }
-        if (p.conj_out) v = A::conj(v);
-        __stcs(out + obase + g0 * p.os[0] + (int64_t)i * p.oes, A::store_s(v, delta_out, p.scale));
-    }
+    };
+    if (p.scale == 1.0) store_all(std::true_type{});
+    else store_all(std::false_type{});
 }
 
 template <class A>

@@ -336,10 +336,22 @@ __device__ __forceinline__ void finish_tile(const tfft_pass &p, const TileGeom &
 
     Store *out = reinterpret_cast<Store *>(p.out) + g.obase;
     if (g.live) {
+        /* scale 1 (every pass but an inverse's last) in a loop of its own,
+         * so the per-element test of the double-precision scale folds away
+         * (it would take an FP64 instruction per point) */
+        if (p.scale == 1.0) {
 #pragma unroll
-        for (int q = 0; q < E; q++) {
-            C v = p.conj_out ? A::conj(a[q]) : a[q];
-            __stcs(out + (int64_t)(j + q * TPL) * p.oes, A::store_s(v, delta_out, p.scale));
+            for (int q = 0; q < E; q++) {
+                C v = p.conj_out ? A::conj(a[q]) : a[q];
+                __stcs(out + (int64_t)(j + q * TPL) * p.oes, A::store_s(v, delta_out, 1.0));
+            }
+        } else {
+            const double scale = p.scale;
+#pragma unroll
+            for (int q = 0; q < E; q++) {
+                C v = p.conj_out ? A::conj(a[q]) : a[q];
+                __stcs(out + (int64_t)(j + q * TPL) * p.oes, A::store_s(v, delta_out, scale));
+            }
         }
     }
 }
