@@ -135,6 +135,14 @@ int tfft_pass_supported(int log_l, int b_tile, int arith, int ept)
     return (log_l + lb) <= (arith == TFFT_ARITH_F32 ? 14 : 13);
 }
 
+/* no stand-in kernel stages tiles with bulk copies: the planner's copy and
+ * launch logs stay those of direct loads */
+int tfft_pass_bulk_capable(int log_l, int b_tile, int arith, int ept)
+{
+    (void)log_l; (void)b_tile; (void)arith; (void)ept;
+    return 0;
+}
+
 int tfft_mixed_supported(int len, int b_tile, int arith)
 {
     int m = len;

@@ -57,6 +57,15 @@ extern "C" int tfft_pass_supported(int log_l, int b_tile, int arith, int ept)
     return tfft::find(log_l, b_tile, arith, ept) != nullptr;
 }
 
+extern "C" int tfft_pass_bulk_capable(int log_l, int b_tile, int arith, int ept)
+{
+    /* bulk_capable() of fft_pass.cuh for the shapes find() launches with the
+     * ordinary pass kernel */
+    if (arith == TFFT_ARITH_TC || (ept != 0 && ept != 16)) return 0;
+    if (b_tile < 8 || log_l < 5 || (int64_t(TFFT_ELEM_BYTES(arith)) << log_l) < 512) return 0;
+    return tfft::find(log_l, b_tile, arith, ept) != nullptr;
+}
+
 extern "C" int tfft_launch_pass(const tfft_pass *p, void *stream)
 {
     if (p->len) return tfft::launch_mixed(*p, (cudaStream_t)stream);

@@ -22,6 +22,7 @@
  * threads reads or writes B*16 contiguous bytes.
  */
 #pragma once
+#include <type_traits>
 #include <utility>
 
 #include "fft_arith.cuh"
@@ -356,12 +357,114 @@ __device__ __forceinline__ void finish_tile(const tfft_pass &p, const TileGeom &
     }
 }
 
+/* kernel shapes that may stage a full tile of contiguous lines with bulk
+ * copies: 16 points per thread, at least 8 lines per tile (a tile of one or
+ * two long lines loads as well directly: measured up to 6% slower staged),
+ * lines of at least 512 bytes (the staging slots then fit the exchange
+ * buffer), the ordinary pass kernel only */
+template <class A, int LOG_L, int B, bool L2ONLY, class LINE, int EPT>
+__host__ __device__ constexpr bool bulk_capable()
+{
+    return !L2ONLY && std::is_same<LINE, CoreLine>::value && EPT == 16 && B >= 8 &&
+           LOG_L >= 5 && ((size_t)1 << LOG_L) * sizeof(typename A::Store) >= 512;
+}
+
+/* bytes of shared memory a launch needs: the exchange buffer, plus the
+ * bulk copies' mbarrier where the shape stages tiles */
+template <class A, int LOG_L, int B, int EPT = 16>
+__host__ __device__ constexpr size_t pass_launch_smem_bytes()
+{
+    return pass_smem_bytes<A, LOG_L, B, EPT>() +
+           (bulk_capable<A, LOG_L, B, false, CoreLine, EPT>() ? 16 : 0);
+}
+
+#ifdef __CUDA_ARCH__
+__device__ __forceinline__ uint32_t smem_addr32(const void *p)
+{
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+/* poll an mbarrier for the phase of parity 0; false if it did not complete
+ * within 2^22 polls */
+__device__ __forceinline__ bool mbar_wait0(uint32_t mbar)
+{
+    for (int it = 0; it < (1 << 22); it++) {
+        uint32_t ok;
+        asm volatile(
+            "{\n.reg .pred P1;\nmbarrier.try_wait.parity.shared::cta.b64 P1, [%1], 0;\n"
+            "selp.b32 %0, 1, 0, P1;\n}\n"
+            : "=r"(ok)
+            : "r"(mbar)
+            : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+#endif
+
 /*
- * One tile, loaded straight into registers.  L2ONLY selects loads that
- * bypass L1 (ld.global.cg): needed when another CTA of the same launch wrote
- * the data (the persistent batch kernel); a plain pass launch reads with the
- * streaming hint.  LINE transforms the loaded points (CoreLine, or the
- * tensor-core stages of fft_tc.cuh).
+ * A full tile of B contiguous lines (ies == 1, is[0] == L) staged through
+ * shared memory: an mbarrier after the exchange buffer, one bulk
+ * asynchronous copy per line (issued by threads 0..B-1, evict-first in L2)
+ * into a slot of L elements plus 32 bytes (the padding spreads the lines'
+ * first elements over the banks), then each thread reads its E points from
+ * its line's slot.
+ * Ends with a barrier: the stages reuse the buffer.  A wait that gives up
+ * sets *p.err and waits once more (bounded) for the copies in flight.
+ */
+template <class A, int LOG_L, int B, int E, int TPL>
+__device__ __forceinline__ void bulk_load_tile(const tfft_pass &p, const TileGeom &g,
+                                               typename A::Store (&raw)[E], unsigned char *smem_raw,
+                                               int j, int b)
+{
+#ifdef __CUDA_ARCH__
+    using Store = typename A::Store;
+    constexpr int L = 1 << LOG_L;
+    constexpr uint32_t LINE_BYTES = (uint32_t)(L * sizeof(Store));
+    constexpr size_t SLOT = (size_t)LINE_BYTES + 32;
+    static_assert(B * SLOT <= pass_smem_bytes<A, LOG_L, B>(), "staging slots inside the exchange buffer");
+    const uint32_t mbar = smem_addr32(smem_raw + pass_smem_bytes<A, LOG_L, B>());
+    const int t = threadIdx.x;
+    if (t == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar),
+                     "r"(B * LINE_BYTES)
+                     : "memory");
+    }
+    __syncthreads();
+    if (t < B) { /* thread t's tile line is line t (b = t % B, t < B) */
+        const Store *src = reinterpret_cast<const Store *>(p.in) + g.ibase;
+        /* evict-first in L2, as the direct path's streaming loads: a pass's
+         * input must not push out the output the next pass reads */
+        asm volatile(
+            "{\n.reg .b64 pol;\n"
+            "createpolicy.fractional.L2::evict_first.b64 pol, 1.0;\n"
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint "
+            "[%0], [%1], %2, [%3], pol;\n}\n" ::"r"(smem_addr32(smem_raw + t * SLOT)),
+            "l"(src), "r"(LINE_BYTES), "r"(mbar)
+            : "memory");
+    }
+    if (!mbar_wait0(mbar)) {
+        if (p.err) atomicExch(p.err, 1);
+        mbar_wait0(mbar);
+    }
+    const Store *ln = reinterpret_cast<const Store *>(smem_raw + b * SLOT);
+#pragma unroll
+    for (int q = 0; q < E; q++) raw[q] = ln[j + q * TPL];
+    __syncthreads();
+#else
+    (void)p; (void)g; (void)raw; (void)smem_raw; (void)j; (void)b;
+#endif
+}
+
+/*
+ * One tile.  L2ONLY selects loads that bypass L1 (ld.global.cg): needed when
+ * another CTA of the same launch wrote the data (the persistent batch
+ * kernel); a plain pass launch reads with the streaming hint, or, for a full
+ * tile of contiguous lines in a shape that takes it (bulk_capable, p.bulk
+ * set), through shared memory by bulk asynchronous copies.  LINE transforms
+ * the loaded points (CoreLine, or the tensor-core stages of fft_tc.cuh).
  */
 template <class A, int LOG_L, int B, bool L2ONLY, class LINE = CoreLine, int EPT = 16>
 __device__ __forceinline__ void run_tile(const tfft_pass &p, int64_t tile, unsigned char *smem_raw,
@@ -375,6 +478,20 @@ __device__ __forceinline__ void run_tile(const tfft_pass &p, int64_t tile, unsig
     const TileGeom g = tile_geom<B>(p, tile, b);
     const Store *in = reinterpret_cast<const Store *>(p.in) + g.ibase;
     Store raw[E];
+#if defined(__CUDA_ARCH__)
+    if constexpr (bulk_capable<A, LOG_L, B, L2ONLY, LINE, EPT>()) {
+        /* CTA-uniform: the pass qualifies, the tile is full, its base is
+         * 16-byte aligned */
+        const int64_t tiles0 = (p.n[0] + B - 1) / B;
+        const int64_t first = (tile % tiles0) * B;
+        const Store *base = reinterpret_cast<const Store *>(p.in) + (g.ibase - (int64_t)b * p.is[0]);
+        if (p.bulk && first + B <= p.n[0] && ((uintptr_t)base & 15) == 0) {
+            bulk_load_tile<A, LOG_L, B, E, TPL>(p, g, raw, smem_raw, j, b);
+            finish_tile<A, LOG_L, B, LINE, EPT>(p, g, raw, sm, j, b, line);
+            return;
+        }
+    }
+#endif
 #pragma unroll
     for (int q = 0; q < E; q++) {
         if constexpr (L2ONLY) {
@@ -411,7 +528,7 @@ template <class A, int LOG_L, int LOG_B, int EPT = 16>
 int launch_pass(const tfft_pass &p, cudaStream_t s)
 {
     constexpr int B = 1 << LOG_B;
-    constexpr size_t smem = pass_smem_bytes<A, LOG_L, B, EPT>();
+    constexpr size_t smem = pass_launch_smem_bytes<A, LOG_L, B, EPT>();
     static unsigned attr_done = 0; /* one bit per device ordinal */
     auto kern = pass_kernel<A, LOG_L, B, EPT>;
     if constexpr (smem > 48 * 1024) {

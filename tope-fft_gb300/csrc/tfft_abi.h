@@ -88,6 +88,13 @@ typedef struct tfft_pass {
     int len;
     int nrad;
     unsigned char radix[TFFT_MAX_RADICES];
+    /* tiles of whole contiguous lines (ies == 1, is[0] == L): a full tile may
+     * arrive by bulk asynchronous copies (cp.async.bulk, one per line) into
+     * shared memory instead of direct loads, in the kernel shapes that take
+     * it (tfft_pass_bulk_capable); err, a device word, is set to 1 when a
+     * wait for those copies gives up (NULL: not reported) */
+    int bulk;
+    int *err;
 } tfft_pass;
 
 /* mixed-radix lines: at most TFFT_MIXED_MAX_POINTS points per CTA (L * b_tile) */
@@ -191,6 +198,8 @@ int tfft_tc_error(int *flag, void *stream);
 int tfft_launch_pass(const tfft_pass *p, void *stream);
 /* can this (log_l, b_tile, arith, points per thread) be launched? */
 int tfft_pass_supported(int log_l, int b_tile, int arith, int ept);
+/* does that kernel shape stage full contiguous tiles with bulk copies? */
+int tfft_pass_bulk_capable(int log_l, int b_tile, int arith, int ept);
 /* can the mixed-radix kernel run lines of len points, b_tile per CTA? */
 int tfft_mixed_supported(int len, int b_tile, int arith);
 /* out[k] = sum_j in[j] W_n^{jk} (dir 1) or conjugate kernel scaled by 1/n,

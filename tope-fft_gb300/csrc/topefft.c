@@ -241,6 +241,8 @@ typedef struct tope_impl {
     void *chirp, *bhat;
     int64_t bl_m;
     void *tc_matrix; /* tensor form: the DFT-16 matrix pieces */
+    int *err_word;   /* device word set when a wait for bulk tile copies gives
+                        up (allocated with the first pass that stages tiles) */
     /* real-data plan (R2C): the complex transform of length m = n/2 runs on
      * the packed reals; spec holds the m + 1 outputs per row */
     int real;
@@ -441,6 +443,15 @@ static int merge_dims(dimref *d, int n)
     return m;
 }
 
+/* TOPEFFT_BULK=0 makes plans load every tile directly instead of staging
+ * full contiguous tiles with bulk copies (the same transform, another load
+ * path: for comparing the two) */
+static int bulk_enabled(void)
+{
+    const char *e = getenv("TOPEFFT_BULK");
+    return !(e && e[0] == '0');
+}
+
 /* one pass over lines of len points (a power of two, or a smooth length for
  * the mixed-radix kernel) */
 static int add_pass(struct topeFFT *f, tope_impl *P, int64_t len, int64_t ies, int64_t oes,
@@ -493,6 +504,22 @@ static int add_pass(struct topeFFT *f, tope_impl *P, int64_t len, int64_t ies, i
         p->mma_b = P->tc_matrix;
     }
     p->b_tile = b;
+    /* whole contiguous lines in a kernel shape that stages full tiles with
+     * bulk asynchronous copies; a wait for them that gives up sets the plan's
+     * device word, which the synchronous Exec reports */
+    if (!mixed && nl > 0 && ies == 1 && p->is[0] == ((int64_t)1 << log_l) && !p->tab0 &&
+        bulk_enabled() && tfft_pass_bulk_capable(log_l, b, P->arith, p->ept)) {
+        if (!P->err_word) {
+            void *w;
+            int st = impl_alloc_tab(P, 16, -1, &w);
+            if (st) return set_status(f, st);
+            int rc = tfft_memset_async(w, 0, 16, f->command_queue);
+            if (rc) return cuda_status(f, rc);
+            P->err_word = (int *)w;
+        }
+        p->bulk = 1;
+        p->err = P->err_word;
+    }
     if (post_tw && P->arith == TFFT_ARITH_F64 && tw_n <= FULL_TW_MAX) {
         /* FP64 butterflies: one load from the whole table W_N^m instead of
          * the product of two table entries saves 4 of the pass's ~45 FP64
@@ -1126,6 +1153,16 @@ static int tc_status(struct topeFFT *f, const tope_impl *P, void *stream)
         int flag = 0, rc;
         if ((rc = tfft_tc_error(&flag, stream))) return cuda_status(f, rc);
         if (flag) return set_status(f, TOPE_ERR_TIMEOUT);
+    }
+    if (P->err_word) { /* a wait for bulk tile copies that gave up */
+        int flag = 0, rc;
+        if ((rc = tfft_d2h(&flag, P->err_word, sizeof(int), stream)) || (rc = tfft_stream_sync(stream)))
+            return cuda_status(f, rc);
+        if (flag) {
+            tfft_memset_async(P->err_word, 0, sizeof(int), stream);
+            tfft_stream_sync(stream);
+            return set_status(f, TOPE_ERR_TIMEOUT);
+        }
     }
     return set_status(f, TOPE_SUCCESS);
 }
