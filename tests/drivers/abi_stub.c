@@ -143,6 +143,14 @@ int tfft_pass_bulk_capable(int log_l, int b_tile, int arith, int ept)
     return 0;
 }
 
+/* no tensor maps in the stand-in: strided passes load directly */
+int tfft_tensor_map(void *dev_map, const void *base, int rank, const int64_t *dims,
+                    const int64_t *strides, const int *box)
+{
+    (void)dev_map; (void)base; (void)rank; (void)dims; (void)strides; (void)box;
+    return 1;
+}
+
 int tfft_mixed_supported(int len, int b_tile, int arith)
 {
     int m = len;

@@ -15,7 +15,7 @@ unsigned g_warp_val[32][32];
 emu_graph *g_capture;
 
 namespace tfft {
-alignas(16) unsigned char smem_raw[1 << 18];
+alignas(128) unsigned char smem_raw[1 << 18];
 LaunchFn launcher_tc(int) { return nullptr; }
 } // namespace tfft
 
@@ -32,4 +32,9 @@ int tfft_tc_error(int *flag, void *)
     return 0;
 }
 int topeExec1DNoAlloc(const double *, double *, int, int, void *) { return TOPE_ERR_UNSUPPORTED; }
+/* no tensor maps on the host: strided passes load directly */
+int tfft_tensor_map(void *, const void *, int, const int64_t *, const int64_t *, const int *)
+{
+    return 1;
+}
 }

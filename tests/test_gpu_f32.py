@@ -108,6 +108,24 @@ def test_f32_full_size(T, fw, orc, dims, batch):
     assert err <= fw.gate
 
 
+@pytest.mark.parametrize("dims,batch", [((128, 128, 128), 1), ((512, 256, 1), 1),
+                                        ((1 << 14, 1, 1), 64), ((64, 32, 256), 1)],
+                         ids=["128^3", "512x256", "64x2^14", "64x32x256"])
+def test_load_paths_agree(T, fw, orc, monkeypatch, dims, batch):
+    """Tiles loaded directly (TOPEFFT_BULK=0), contiguous tiles by bulk
+    copies (1, the default) and strided tiles by TMA boxes from tensor maps
+    as well (2): the same transform bit for bit, and within the gate."""
+    x = pulse_field(orc, dims, batch)
+    x32 = x.astype(np.float32)
+    outs = []
+    for level in ("0", "1", "2"):
+        monkeypatch.setenv("TOPEFFT_BULK", level)
+        outs.append(run_f32(T, fw, x32, dims, 1, batch))
+    assert np.array_equal(outs[0], outs[1]) and np.array_equal(outs[0], outs[2])
+    err = orc.rel_l2(outs[2].astype(np.float64), oracle_fp64(orc, x, dims, 1, batch))
+    assert err <= fw.gate
+
+
 def test_f32_round_trip_and_type_checks(T, fw, orc):
     n, b = 1 << 15, 8
     x32 = orc.uniform(n * b, 3).astype(np.float32)

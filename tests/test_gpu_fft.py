@@ -283,6 +283,23 @@ def test_nd_full_size(T, fw, orc, shape):
     assert orc.rel_l2(d, x) <= tol
 
 
+@pytest.mark.parametrize("shape", [(64, 64, 64), (256, 128, 1), (32, 16, 512)],
+                         ids=["64^3", "256x128", "32x16x512"])
+def test_load_paths_agree(T, fw, orc, monkeypatch, shape):
+    """Direct tile loads (TOPEFFT_BULK=0), bulk copies of contiguous tiles
+    (1, the default) and TMA boxes for strided tiles as well (2) give the
+    same transform bit for bit, at the oracle's gate."""
+    nx, ny, nz = shape
+    x = orc.uniform(nx * ny * nz, SEED0 + 21)
+    outs = []
+    for level in ("0", "1", "2"):
+        monkeypatch.setenv("TOPEFFT_BULK", level)
+        outs.append(run_nd(T, fw, x, shape))
+    assert np.array_equal(outs[0], outs[1]) and np.array_equal(outs[0], outs[2])
+    ref = orc.exec(x, nx, ny, nz, 1)
+    assert orc.rel_l2(outs[2], ref) <= tol_fp64(nx * ny * nz)
+
+
 def test_per_axis_exec(T, fw, orc):
     """tope2DExecX then tope2DExecY == the X and Y passes of a forward Exec."""
     nx, ny = 64, 32

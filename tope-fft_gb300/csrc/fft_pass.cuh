@@ -459,6 +459,84 @@ __device__ __forceinline__ void bulk_load_tile(const tfft_pass &p, const TileGeo
 }
 
 /*
+ * A full tile of B adjacent strided lines (is[0] == 1) staged by TMA: the
+ * pass's tensor map (p.tmap, dimension 0 the lines) gives one box per 256
+ * elements of the line, issued by threads 0..NCH-1 with an evict-first L2
+ * policy; the boxes land as rows of B elements, row i of the tile at
+ * i * B elements, so thread (j, b) reads element (j + q * TPL) * B + b and a
+ * warp reads consecutive words.  Bounded wait and error word as
+ * bulk_load_tile; ends with a barrier.
+ */
+template <class A, int LOG_L, int B, int E, int TPL>
+__device__ __forceinline__ void tma_load_tile(const tfft_pass &p, int64_t tile, int64_t first,
+                                              typename A::Store (&raw)[E], unsigned char *smem_raw,
+                                              int j, int b)
+{
+#ifdef __CUDA_ARCH__
+    using Store = typename A::Store;
+    constexpr int L = 1 << LOG_L;
+    constexpr int ROWS = L < 256 ? L : 256, NCH = L / ROWS;
+    constexpr uint32_t CH_BYTES = (uint32_t)(ROWS * B * sizeof(Store));
+    static_assert((size_t)L * B * sizeof(Store) <= pass_smem_bytes<A, LOG_L, B>(),
+                  "tile inside the exchange buffer");
+    static_assert(CH_BYTES % 128 == 0, "boxes on 128-byte boundaries");
+    const uint32_t mbar = smem_addr32(smem_raw + pass_smem_bytes<A, LOG_L, B>());
+    const int t = threadIdx.x;
+    if (t == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar),
+                     "r"((uint32_t)NCH * CH_BYTES)
+                     : "memory");
+    }
+    __syncthreads();
+    if (t < NCH) {
+        const int64_t tiles0 = (p.n[0] + B - 1) / B;
+        const int64_t rest = tile / tiles0;
+        const int64_t src[3] = {(int64_t)t * ROWS, rest % p.n[1], rest / p.n[1]};
+        int c[4] = {(int)(first * (int64_t)(sizeof(Store) / 8)), 0, 0, 0};
+#pragma unroll
+        for (int k = 1; k < 4; k++)
+            if (k < p.tmap_rank) c[k] = (int)src[p.tmap_src[k - 1]];
+        const uint32_t dst = smem_addr32(smem_raw + t * CH_BYTES);
+        const unsigned long long map = (unsigned long long)p.tmap;
+        if (p.tmap_rank == 2) {
+            asm volatile(
+                "{\n.reg .b64 pol;\ncreatepolicy.fractional.L2::evict_first.b64 pol, 1.0;\n"
+                "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint"
+                " [%0], [%1, {%2, %3}], [%4], pol;\n}\n" ::"r"(dst),
+                "l"(map), "r"(c[0]), "r"(c[1]), "r"(mbar)
+                : "memory");
+        } else if (p.tmap_rank == 3) {
+            asm volatile(
+                "{\n.reg .b64 pol;\ncreatepolicy.fractional.L2::evict_first.b64 pol, 1.0;\n"
+                "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint"
+                " [%0], [%1, {%2, %3, %4}], [%5], pol;\n}\n" ::"r"(dst),
+                "l"(map), "r"(c[0]), "r"(c[1]), "r"(c[2]), "r"(mbar)
+                : "memory");
+        } else {
+            asm volatile(
+                "{\n.reg .b64 pol;\ncreatepolicy.fractional.L2::evict_first.b64 pol, 1.0;\n"
+                "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint"
+                " [%0], [%1, {%2, %3, %4, %5}], [%6], pol;\n}\n" ::"r"(dst),
+                "l"(map), "r"(c[0]), "r"(c[1]), "r"(c[2]), "r"(c[3]), "r"(mbar)
+                : "memory");
+        }
+    }
+    if (!mbar_wait0(mbar)) {
+        if (p.err) atomicExch(p.err, 1);
+        mbar_wait0(mbar);
+    }
+    const Store *rows = reinterpret_cast<const Store *>(smem_raw);
+#pragma unroll
+    for (int q = 0; q < E; q++) raw[q] = rows[(j + q * TPL) * B + b];
+    __syncthreads();
+#else
+    (void)p; (void)tile; (void)first; (void)raw; (void)smem_raw; (void)j; (void)b;
+#endif
+}
+
+/*
  * One tile.  L2ONLY selects loads that bypass L1 (ld.global.cg): needed when
  * another CTA of the same launch wrote the data (the persistent batch
  * kernel); a plain pass launch reads with the streaming hint, or, for a full
@@ -480,11 +558,16 @@ __device__ __forceinline__ void run_tile(const tfft_pass &p, int64_t tile, unsig
     Store raw[E];
 #if defined(__CUDA_ARCH__)
     if constexpr (bulk_capable<A, LOG_L, B, L2ONLY, LINE, EPT>()) {
-        /* CTA-uniform: the pass qualifies, the tile is full, its base is
-         * 16-byte aligned */
+        /* CTA-uniform: the pass qualifies, the tile is full (and for the
+         * contiguous path, its base is 16-byte aligned) */
         const int64_t tiles0 = (p.n[0] + B - 1) / B;
         const int64_t first = (tile % tiles0) * B;
         const Store *base = reinterpret_cast<const Store *>(p.in) + (g.ibase - (int64_t)b * p.is[0]);
+        if (p.tmap && first + B <= p.n[0]) {
+            tma_load_tile<A, LOG_L, B, E, TPL>(p, tile, first, raw, smem_raw, j, b);
+            finish_tile<A, LOG_L, B, LINE, EPT>(p, g, raw, sm, j, b, line);
+            return;
+        }
         if (p.bulk && first + B <= p.n[0] && ((uintptr_t)base & 15) == 0) {
             bulk_load_tile<A, LOG_L, B, E, TPL>(p, g, raw, smem_raw, j, b);
             finish_tile<A, LOG_L, B, LINE, EPT>(p, g, raw, sm, j, b, line);
@@ -520,7 +603,7 @@ __global__ void
 __launch_bounds__(Shape<LOG_L, EPT>::TPL * B, pass_min_blocks<A, Shape<LOG_L, EPT>::TPL * B>())
     pass_kernel(const tfft_pass p)
 {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    extern __shared__ __align__(128) unsigned char smem_raw[]; /* TMA boxes: 128-byte aligned */
     run_tile<A, LOG_L, B, false, CoreLine, EPT>(p, blockIdx.x, smem_raw);
 }
 

@@ -95,6 +95,15 @@ typedef struct tfft_pass {
      * wait for those copies gives up (NULL: not reported) */
     int bulk;
     int *err;
+    /* strided passes of adjacent lines (is[0] == 1): a tensor map of the
+     * pass's input array (device memory, TFFT_TENSOR_MAP_BYTES) in 8-byte
+     * units, dimension 0 the lines, dimension k + 1 the source tmap_src[k]
+     * (0: the line's elements, 1: g1, 2: g2) in stride order; full tiles
+     * then arrive by TMA, boxes of the tile's lines by up to 256 elements
+     * (NULL: not used) */
+    const void *tmap;
+    int tmap_rank;
+    signed char tmap_src[4];
 } tfft_pass;
 
 /* mixed-radix lines: at most TFFT_MIXED_MAX_POINTS points per CTA (L * b_tile) */
@@ -200,6 +209,13 @@ int tfft_launch_pass(const tfft_pass *p, void *stream);
 int tfft_pass_supported(int log_l, int b_tile, int arith, int ept);
 /* does that kernel shape stage full contiguous tiles with bulk copies? */
 int tfft_pass_bulk_capable(int log_l, int b_tile, int arith, int ept);
+/* encode a tiled tensor map of 8-byte elements (rank 2..5, dims and box per
+ * dimension, strides in bytes of dimensions 1..rank-1) over base and copy it
+ * to dev_map (TFFT_TENSOR_MAP_BYTES of device memory); nonzero when the
+ * driver lacks the call or the layout does not fit its rules */
+#define TFFT_TENSOR_MAP_BYTES 128
+int tfft_tensor_map(void *dev_map, const void *base, int rank, const int64_t *dims,
+                    const int64_t *strides, const int *box);
 /* can the mixed-radix kernel run lines of len points, b_tile per CTA? */
 int tfft_mixed_supported(int len, int b_tile, int arith);
 /* out[k] = sum_j in[j] W_n^{jk} (dir 1) or conjugate kernel scaled by 1/n,

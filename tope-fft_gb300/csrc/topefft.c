@@ -241,8 +241,12 @@ typedef struct tope_impl {
     void *chirp, *bhat;
     int64_t bl_m;
     void *tc_matrix; /* tensor form: the DFT-16 matrix pieces */
-    int *err_word;   /* device word set when a wait for bulk tile copies gives
-                        up (allocated with the first pass that stages tiles) */
+    int *err_word;   /* device word set when a wait for bulk or TMA tile copies
+                        gives up (allocated with the first pass that stages tiles) */
+    /* strided passes of adjacent lines that may stage tiles by TMA, and their
+     * tensor maps over buf[0] and buf[1] (NULL where none was built) */
+    int tma_cand[MAX_PASSES];
+    void *tmap_dev[MAX_PASSES][2];
     /* real-data plan (R2C): the complex transform of length m = n/2 runs on
      * the packed reals; spec holds the m + 1 outputs per row */
     int real;
@@ -443,13 +447,15 @@ static int merge_dims(dimref *d, int n)
     return m;
 }
 
-/* TOPEFFT_BULK=0 makes plans load every tile directly instead of staging
- * full contiguous tiles with bulk copies (the same transform, another load
- * path: for comparing the two) */
-static int bulk_enabled(void)
+/* How plans load full tiles (the same transform, other load paths: for
+ * comparing them).  TOPEFFT_BULK=0: every tile directly; 1 (the default):
+ * tiles of contiguous lines by bulk copies, strided ones directly; 2: strided
+ * tiles by TMA boxes from tensor maps as well (measured 1.5-4% slower than
+ * direct loads on the FP32 and double-float 3D shapes) */
+static int bulk_level(void)
 {
     const char *e = getenv("TOPEFFT_BULK");
-    return !(e && e[0] == '0');
+    return !e || !e[0] ? 1 : e[0] == '0' ? 0 : e[0] == '2' ? 2 : 1;
 }
 
 /* one pass over lines of len points (a power of two, or a smooth length for
@@ -508,7 +514,7 @@ static int add_pass(struct topeFFT *f, tope_impl *P, int64_t len, int64_t ies, i
      * bulk asynchronous copies; a wait for them that gives up sets the plan's
      * device word, which the synchronous Exec reports */
     if (!mixed && nl > 0 && ies == 1 && p->is[0] == ((int64_t)1 << log_l) && !p->tab0 &&
-        bulk_enabled() && tfft_pass_bulk_capable(log_l, b, P->arith, p->ept)) {
+        bulk_level() >= 1 && tfft_pass_bulk_capable(log_l, b, P->arith, p->ept)) {
         if (!P->err_word) {
             void *w;
             int st = impl_alloc_tab(P, 16, -1, &w);
@@ -519,6 +525,11 @@ static int add_pass(struct topeFFT *f, tope_impl *P, int64_t len, int64_t ies, i
         }
         p->bulk = 1;
         p->err = P->err_word;
+    } else if (!mixed && nl > 0 && ies != 1 && p->is[0] == 1 && !p->tab0 && bulk_level() >= 2 &&
+               tfft_pass_bulk_capable(log_l, b, P->arith, p->ept)) {
+        /* adjacent strided lines: TMA boxes from a tensor map, built once
+         * the plan's buffers exist (plan_tensor_maps) */
+        P->tma_cand[P->npass] = 1;
     }
     if (post_tw && P->arith == TFFT_ARITH_F64 && tw_n <= FULL_TW_MAX) {
         /* FP64 butterflies: one load from the whole table W_N^m instead of
@@ -681,6 +692,70 @@ static int plan_split(struct topeFFT *f, tope_impl *P, int64_t n, int parts, int
     d[nl].out_stride = oes;
     d[nl].is_twiddle = 0;
     return plan_split(f, P, n1, parts - 1, ies, oes * n2, d, nl + 1);
+}
+
+/*
+ * Tensor maps for the passes marked in tma_cand, one per allocated buffer
+ * (a pass reads buf[cur], which alternates where the plan has out-of-place
+ * passes).  The map is the pass's input array in 8-byte units: dimension 0
+ * the adjacent lines (n[0] * S / 8 units), then the line's elements (L,
+ * stride ies) and the other line dimensions (n[1], n[2]) in stride order;
+ * the strides must nest and be multiples of 16 bytes.  A pass whose layout
+ * does not fit, or a driver without the call, keeps direct loads; only an
+ * allocation failure is an error.
+ */
+static int plan_tensor_maps(struct topeFFT *f, tope_impl *P)
+{
+    const int64_t u = P->es / 8; /* 8-byte units per element */
+    for (int i = 0; i < P->npass; i++) {
+        tfft_pass *p = &P->pass[i];
+        if (!P->tma_cand[i] || p->tab1) continue;
+        int64_t cnt[3] = {(int64_t)1 << p->log_l, p->n[1], p->n[2]};
+        int64_t str[3] = {p->ies * P->es, p->is[1] * P->es, p->is[2] * P->es};
+        int ord[3], no = 0;
+        for (int k = 0; k < 3; k++)
+            if (k == 0 || cnt[k] > 1) ord[no++] = k;
+        for (int a = 1; a < no; a++) /* by stride */
+            for (int c = a; c > 0 && str[ord[c]] < str[ord[c - 1]]; c--) {
+                int tmp = ord[c];
+                ord[c] = ord[c - 1];
+                ord[c - 1] = tmp;
+            }
+        int64_t dims[4], strides[3];
+        int box[4];
+        dims[0] = p->n[0] * u;
+        box[0] = p->b_tile * (int)u;
+        int ok = 1;
+        int64_t extent = dims[0] * 8;
+        for (int k = 0; k < no; k++) {
+            dims[k + 1] = cnt[ord[k]];
+            strides[k] = str[ord[k]];
+            box[k + 1] = ord[k] == 0 ? (cnt[0] < 256 ? (int)cnt[0] : 256) : 1;
+            if (strides[k] < extent || strides[k] % 16) ok = 0;
+            extent = strides[k] * dims[k + 1];
+            p->tmap_src[k] = (signed char)ord[k];
+        }
+        if (!ok) continue;
+        p->tmap_rank = no + 1;
+        for (int k = 0; k < 2; k++) {
+            if (!P->buf[k]) continue;
+            void *map;
+            int st = impl_alloc_tab(P, TFFT_TENSOR_MAP_BYTES, -1, &map);
+            if (st) return set_status(f, st);
+            if (tfft_tensor_map(map, P->buf[k], p->tmap_rank, dims, strides, box)) continue;
+            P->tmap_dev[i][k] = map;
+        }
+        if ((P->tmap_dev[i][0] || P->tmap_dev[i][1]) && !P->err_word) {
+            void *w;
+            int st = impl_alloc_tab(P, 16, -1, &w);
+            if (st) return set_status(f, st);
+            int rc = tfft_memset_async(w, 0, 16, f->command_queue);
+            if (rc) return cuda_status(f, rc);
+            P->err_word = (int *)w;
+        }
+        p->err = P->err_word;
+    }
+    return TOPE_SUCCESS;
 }
 
 /* passes for one axis (0 = x, 1 = y, 2 = z) */
@@ -891,6 +966,7 @@ static int impl_create(struct topeFFT *f, tope_impl **out, int ndim, int64_t x, 
         int need2 = 0;
         for (int i = 0; i < P->npass; i++) need2 |= P->oop[i];
         if (!st && need2 && tfft_malloc(&P->buf[1], bytes)) st = set_status(f, TOPE_ERR_ALLOC);
+        if (!st) st = plan_tensor_maps(f, P);
         /* per-axis bit-reversal and quarter-wave tables of the reference's plan */
         for (int a = spec ? 1 : 0; a < ndim && !st; a++) {
             int lg = ilog2_exact64(P->c[a]);
@@ -1024,6 +1100,7 @@ static tfft_pass pass_args(const tope_impl *P, int i, int first, int last, int d
 {
     tfft_pass p = P->pass[i];
     p.in = P->buf[P->cur];
+    p.tmap = P->tmap_dev[i][P->cur];
     p.out = P->oop[i] ? P->buf[1 - P->cur] : P->buf[P->cur];
     p.conj_in = (dir == INVERSE) && (i == first);
     p.conj_out = (dir == INVERSE) && (i == last);
@@ -1263,6 +1340,7 @@ static int rb_run(struct topeFFT *f, tope_impl *P, const rb_geom *g, int dir, do
     int ns = 0, rc;
     for (int64_t a = 0; a < n; a += g->step, ns++) {
         tfft_pass q = p;
+        q.tmap = NULL; /* the map covers the whole array, not the slice */
         q.n[g->dim] = (a + g->step <= n) ? g->step : n - a;
         q.in = (const char *)p.in + (size_t)(a * p.is[g->dim]) * es;
         q.out = (char *)p.out + (size_t)(a * p.os[g->dim]) * es;
