@@ -229,5 +229,9 @@ int main(int argc, char **argv)
     if (want(12)) mixed<ArithF64>(12, {243, 2, 3, false, 1, false, 1.0, 3, 1}, 1e-14);
     if (want(13)) mixed<ArithDF64>(13, {81, 4, 5, true, 2, true, 1.0, 3, 1}, 1e-13);
     if (want(14)) pass<ArithF64, 8, 2, 16>(14, {256, 2, 3, false, 1, false, 1.0, 4, 1}, 1e-14);
+    /* double-float lines of three and four stages: the stages after the
+     * first run as a loop with the stage index at run time */
+    if (want(15)) pass<ArithDF32, 9, 8, 16>(15, {512, 8, 16, true, 1, false, 1.0}, 1e-7);
+    if (want(16)) pass<ArithDF64, 11, 2, 16>(16, {2048, 2, 4, false, 0, true, 1.0}, 1e-13);
     return 0;
 }

@@ -30,7 +30,7 @@ from conftest import ROOT
 CSRC = ROOT / "tope-fft_gb300" / "csrc"
 EMU = ROOT / "tests" / "emu"
 HEADERS = ["fft_pass.cuh", "fft_mixed.cuh", "fft_arith.cuh", "tfft_abi.h", "fft_mixed_consts.inc"]
-NCASES = 15
+NCASES = 17
 NAUX = 7
 
 

@@ -16,6 +16,13 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+/* a function kept out of line (a rare path called from many unrolled sites) */
+#if defined(__CUDACC__)
+#define TFFT_NOINLINE __noinline__
+#else
+#define TFFT_NOINLINE __attribute__((noinline))
+#endif
+
 namespace tfft {
 
 /* cos(pi/8), sin(pi/8), sqrt(1/2): nearest doubles */
@@ -184,89 +191,134 @@ __host__ __device__ __forceinline__ unsigned dexp(double v)
     return (unsigned)(d2ull(v) >> 52) & 0x7ffu;
 }
 
+/* nearest integer (ties to even) of x, |x| < 2^31 */
+__host__ __device__ __forceinline__ int f2i_rn(float x)
+{
+#ifdef __CUDA_ARCH__
+    return __float2int_rn(x);
+#else
+    return (int)__builtin_nearbyint((double)x);
+#endif
+}
+
 /*
  * v * 2^-delta as a (hi, lo) FP32 pair, with integer operations only (no
  * FP64 instruction).  hi keeps the top 24 significant bits (truncated), lo
  * the next 23; the 6 lowest mantissa bits are dropped (relative error below
  * 2^-46).  Values more than 2^100 below 2^delta become 0: delta is the
  * tile's largest exponent, so they are far below the tile's rounding level.
+ * hi comes from the high word shifted left by 3 (the exponent's low 9 bits
+ * over FP32's exponent field, the top 23 mantissa bits below it): adding the
+ * bias change 127 - 1023 - delta to that field and keeping its low 8 bits
+ * gives E + 127, which lies in 27..127.
  */
 __host__ __device__ __forceinline__ void split_double(double v, int delta, float &hi, float &lo)
 {
     const unsigned long long b = d2ull(v);
-    const int e = (int)((b >> 52) & 0x7ffu);
     const unsigned hw = (unsigned)(b >> 32), lw = (unsigned)b;
-    const int E = e - 1023 - delta;
-    const unsigned sign = hw & 0x80000000u;
+    const int e = (int)((hw >> 20) & 0x7ffu);
     /* zeros and FP64 subnormals: a tile that can hold a subnormal within
      * 2^100 of its largest value is lifted by 2^600 before the split (see
      * run_tile), so here they are always far below the tile's rounding level */
-    if (e == 0 || E < -100) {
+    if (e == 0 || e - 1023 - delta < -100) {
         hi = 0.f;
         lo = 0.f;
         return;
     }
-    hi = u2f(sign | ((unsigned)(E + 127) << 23) | ((hw & 0xfffffu) << 3) | (lw >> 29));
-    const unsigned cexp = (unsigned)(E - 23 + 127) << 23;
-    lo = sub_rn(u2f(sign | cexp | ((lw & 0x1fffffffu) >> 6)), u2f(sign | cexp));
+    const unsigned top = (hw << 3) | (lw >> 29);
+    const unsigned hb = ((top + ((unsigned)(127 - 1023 - delta) << 23)) & 0x7fffffffu) | (hw & 0x80000000u);
+    const unsigned base = (hb & 0xff800000u) - (23u << 23); /* sign, 2^(E - 23) */
+    hi = u2f(hb);
+    lo = sub_rn(u2f(base | ((lw >> 6) & 0x7fffffu)), u2f(base));
 }
 
 /*
- * (hi + lo) * 2^delta rounded to the nearest double, with one two-sum on
- * the FP32 pipe and integer operations for the rest.
+ * (s + e) * 2^delta for a renormalised pair (|e| <= ulp(s)/2) in every case
+ * the fast join leaves out: FP32-subnormal parts, FP64-subnormal and
+ * overflowing results (infinities and NaNs give infinity).  The sum is formed
+ * in a 64-bit integer S in units of 2^(es - 182) (s's 24 bits shifted up by
+ * 32; e's bits below the unit folded into a sticky bit), then rounded once,
+ * to nearest even, to the 53 bits of a normal result or the fewer bits of a
+ * subnormal one.
+ */
+static __host__ __device__ TFFT_NOINLINE double join_double_any(float s, float e, int delta)
+{
+    const unsigned sb = f2u(s), eb = f2u(e);
+    if ((sb & 0x7fffffffu) == 0) return 0.0;
+    const unsigned long long sgn = (unsigned long long)(sb & 0x80000000u) << 32;
+    const int es = (int)((sb >> 23) & 0xffu);
+    if (es == 255) return ull2d(sgn | 0x7ff0000000000000ull);
+    const int esn = es ? es : 1;
+    long long S = (long long)((sb & 0x7fffffu) | (es ? 0x800000u : 0u)) << 32;
+    if (eb & 0x7fffffffu) {
+        const int ee = (int)((eb >> 23) & 0xffu);
+        const unsigned long long Me = (eb & 0x7fffffu) | (ee ? 0x800000u : 0u);
+        const int d = esn - (ee ? ee : 1); /* at least 24 */
+        unsigned long long term;
+        if (d <= 32) term = Me << (32 - d);
+        else if (d - 32 < 64) term = (Me >> (d - 32)) | ((Me & ((1ull << (d - 32)) - 1)) ? 1ull : 0ull);
+        else term = 1; /* a sticky bit only */
+        S += ((sb ^ eb) & 0x80000000u) ? -(long long)term : (long long)term;
+    }
+    const int top = 63 - clz64((unsigned long long)S);
+    long long be = (long long)esn - 182 + top + delta + 1023; /* biased exponent at 53 bits */
+    int sh = top - 52;
+    if (be <= 0) sh += (int)(1 - be); /* a subnormal result keeps fewer bits */
+    unsigned long long m;
+    if (sh <= 0) {
+        m = (unsigned long long)S << (-sh);
+    } else if (sh >= 64) {
+        m = 0;
+    } else {
+        const unsigned long long u = (unsigned long long)S;
+        const unsigned long long half = 1ull << (sh - 1), rem = u & ((half << 1) - 1);
+        m = u >> sh;
+        if (rem > half || (rem == half && (m & 1))) m++;
+    }
+    /* a subnormal (or, after a carry, the smallest normal) encodes as m */
+    if (be <= 0) return ull2d(sgn | m);
+    if (m >> 53) { /* the rounding carried into a new binade */
+        m >>= 1;
+        be++;
+    }
+    if (be >= 2047) return ull2d(sgn | 0x7ff0000000000000ull);
+    return ull2d(sgn | ((unsigned long long)be << 52) | (m & 0xfffffffffffffull));
+}
+
+/*
+ * (hi + lo) * 2^delta rounded to the nearest double (ties to even), on the
+ * FP32 pipe and integer units only.  After a two-sum, s + e == hi + lo with
+ * |e| <= ulp(s)/2.  s's bits, shifted into FP64 position with the exponent
+ * rebiased, are the result's top 24 bits; e rounded to the result's unit
+ * (one scale by a power of two in its exponent field and one
+ * float-to-integer conversion, at most 2^28 in magnitude) is added to that
+ * bit pattern as an integer.  When s is a power of two and e points the
+ * other way, the result lies in the binade below, whose unit is half as
+ * large: e is rounded to that unit and the subtraction borrows from the
+ * exponent field, which is exactly that binade's encoding.  s below 2^-71
+ * (where e could be an FP32 subnormal that matters), zeros, infinities and
+ * results near the ends of FP64's exponent range take join_double_any.
  */
 __host__ __device__ __forceinline__ double join_double(float hi, float lo, int delta)
 {
-    /* renormalise: s + e == hi + lo exactly, |e| <= ulp(s)/2 */
-    const float s = add_rn(hi, lo);
-    const float bb = sub_rn(s, hi);
-    const float e = add_rn(sub_rn(hi, sub_rn(s, bb)), sub_rn(lo, bb));
+    float s, e;
+    {
+        s = add_rn(hi, lo);
+        const float bb = sub_rn(s, hi);
+        e = add_rn(sub_rn(hi, sub_rn(s, bb)), sub_rn(lo, bb));
+    }
     const unsigned sb = f2u(s), eb = f2u(e);
-    if ((sb & 0x7fffffffu) == 0) return 0.0;
     const int es = (int)((sb >> 23) & 0xffu);
-    /* s = Ms * 2^(es-150); keep everything in units of 2^(es-179) */
-    long long S = (long long)(((sb & 0x7fffffu) | (es ? 0x800000u : 0u))) << 29;
-    if (eb & 0x7fffffffu) {
-        const int ee = (int)((eb >> 23) & 0xffu);
-        const long long Me = (long long)((eb & 0x7fffffu) | (ee ? 0x800000u : 0u));
-        const int d = (es ? es : 1) - (ee ? ee : 1);
-        long long term = d <= 29 ? (Me << (29 - d)) : (d - 29 < 63 ? (Me >> (d - 29)) : 0);
-        S += ((sb ^ eb) & 0x80000000u) ? -term : term;
-    }
-    /* normalise S into [2^52, 2^53) */
-    const int top = 63 - clz64((unsigned long long)S);
-    int exp2 = (es ? es : 1) - 150 - 29 + 52; /* exponent of the unit of S, plus 52 */
-    unsigned long long m;
-    if (top > 52) {
-        const int sh = top - 52;
-        const unsigned long long u = (unsigned long long)S;
-        const unsigned long long half = 1ull << (sh - 1);
-        const unsigned long long rem = u & ((1ull << sh) - 1);
-        m = u >> sh;
-        if (rem > half || (rem == half && (m & 1))) m++;
-        exp2 += sh;
-    } else {
-        m = (unsigned long long)S << (52 - top);
-        exp2 -= 52 - top;
-    }
-    const long long be = (long long)exp2 + delta + 1023;
-    if (be <= 0) {
-        /* FP64 subnormal result: shift the 53-bit significand into place,
-         * round to nearest even (a carry into bit 52 yields the smallest
-         * normal, as it should) */
-        const long long sh = 1 - be;
-        unsigned long long r = 0;
-        if (sh <= 53) {
-            const unsigned long long half = 1ull << (sh - 1);
-            const unsigned long long rem = m & ((half << 1) - 1);
-            r = m >> sh;
-            if (rem > half || (rem == half && (r & 1))) r++;
-        }
-        return ull2d(((unsigned long long)(sb & 0x80000000u) << 32) | r);
-    }
-    if (be >= 2047) return ull2d(((unsigned long long)(sb & 0x80000000u) << 32) | 0x7ff0000000000000ull);
-    return ull2d(((unsigned long long)(sb & 0x80000000u) << 32) +
-                 ((unsigned long long)be << 52) + (m - (1ull << 52)));
+    const int bexp = es + 896 + delta; /* the result's biased FP64 exponent */
+    if (es < 56 || es == 255 || bexp < 2 || bexp > 2045) return join_double_any(s, e, delta);
+    const int ee = (int)((eb >> 23) & 0xffu);
+    const bool below = ((sb & 0x7fffffu) == 0) && ((sb ^ eb) & 0x80000000u) && ee != 0;
+    const int ek = ee + 179 - es + (below ? 1 : 0); /* e's exponent field in result units */
+    const int t = (ee != 0 && ek > 0) ? f2i_rn(u2f((eb & 0x807fffffu) | ((unsigned)ek << 23))) : 0;
+    const unsigned long long mag = ((unsigned long long)(sb & 0x7fffffffu) << 29) +
+                                   ((unsigned long long)(896 + delta) << 52);
+    const long long ts = (sb & 0x80000000u) ? -(long long)t : (long long)t;
+    return ull2d((mag + (unsigned long long)ts) | ((unsigned long long)(sb & 0x80000000u) << 32));
 }
 
 struct df2 {

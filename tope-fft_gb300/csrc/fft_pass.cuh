@@ -10,8 +10,9 @@
  *     2^(LOG_L mod 4) and then radix-16 stages, each a register butterfly
  *     preceded by W_{Ns*R}^{r*k} twiddles from a per-L table (one rounding
  *     per factor, sincospi in FP64); stages exchange through shared memory
- *     laid out as (p + p/16) * B + b, which keeps 16-byte accesses free of
- *     bank conflicts for every stage;
+ *     laid out as (q + q/16) * B + b, q = p with low bits flipped per shape
+ *     (sidx), which keeps every stage's reads and writes free of bank
+ *     conflicts;
  *   - the result comes out in natural order in the same registers, so no
  *     bit-reversal permutation pass is needed;
  *   - fused on the way out: optional four-step twiddle, conjugation and the
@@ -131,9 +132,43 @@ __device__ __forceinline__ unsigned tile_max_exp(const double2 (&raw)[E])
     }
 }
 
-/* padded shared-memory index of element p of tile line b */
-template <int B>
-__device__ __forceinline__ int sidx(int p, int b) { return (p + (p >> 4)) * B + b; }
+/*
+ * Bit flips of the exchange layout, as source bits for target bits 0, 1, 2
+ * (a | b << 4 | c << 8, 0 = no flip), for a first stage of radix 2^lr0 and
+ * rows of w 8-byte words.  A warp's shared-memory request is served in
+ * 128-byte phases covering 16 / w rows; those rows must land in distinct
+ * groups of w words.  Reads (p = j + q * TPL) step rows by one; the
+ * first stage's writes (p = 2^lr0 * jj + r) step them by 2^lr0, which puts
+ * all rows of a phase in one group.  Flipping low bits by the bits those
+ * writes step through separates both patterns.  The table is the minimum
+ * found by a bank model of every stage's reads and writes for each L and
+ * row width the kernels use; rows of 1 word and of 16 or more need none.
+ */
+__host__ __device__ constexpr int exch_flip(int lr0, int w)
+{
+    return lr0 == 0 ? 0
+         : w == 8   ? lr0
+         : w == 4   ? (lr0 == 1 ? 0x002 : lr0 == 2 ? 0x032 : 0x030)
+         : w == 2   ? (lr0 == 1 ? 0x003 : lr0 == 2 ? 0x030 : 0x300)
+                    : 0;
+}
+
+/* shared-memory index of element p of tile line b (elements of ES bytes,
+ * EPT points per thread): row q + q/16 with q = p after the bit flips of
+ * exch_flip, column b.  The pad row every 16 keeps the radix-16 stages'
+ * accesses, which step by 16 rows, in distinct bank groups. */
+template <int LOG_L, int B, int ES, int EPT = 16>
+__host__ __device__ __forceinline__ int sidx(int p, int b)
+{
+    constexpr int LR0 = (EPT == 16 && LOG_L > 4) ? LOG_L % 4 : 0;
+    constexpr int F = exch_flip(LR0, B * ES / 8);
+    constexpr int FA = F & 15, FB = (F >> 4) & 15, FC = F >> 8;
+    int q = p;
+    if constexpr (FA != 0) q ^= (p >> FA) & 1;
+    if constexpr (FB != 0) q ^= ((p >> FB) & 1) << 1;
+    if constexpr (FC != 0) q ^= ((p >> FC) & 1) << 2;
+    return (q + (q >> 4)) * B + b;
+}
 
 /* Stage structure of a line of 2^LOG_L points, EPT (16 or 4) points per
  * thread: an optional first stage of radix 2^(LOG_L mod log2 EPT), then
@@ -174,7 +209,7 @@ __device__ __forceinline__ void stage(typename A::C *a, typename A::S *sm, int j
     constexpr int L = SH::L, E = SH::E, TPL = SH::TPL;
     if constexpr (FROM_SMEM) {
 #pragma unroll
-        for (int q = 0; q < E; q++) a[q] = A::from_smem(sm[sidx<B>(j + q * TPL, b)]);
+        for (int q = 0; q < E; q++) a[q] = A::from_smem(sm[sidx<LOG_L, B, sizeof(typename A::S), EPT>(j + q * TPL, b)]);
     }
 #pragma unroll
     for (int u = 0; u < E / R; u++) {
@@ -199,7 +234,8 @@ __device__ __forceinline__ void stage(typename A::C *a, typename A::S *sm, int j
             const int k = jj & (NS - 1);
             const int o = (jj / NS) * NS * R + k;
 #pragma unroll
-            for (int r = 0; r < R; r++) sm[sidx<B>(o + r * NS, b)] = A::to_smem(a[u + r * (E / R)]);
+            for (int r = 0; r < R; r++)
+                sm[sidx<LOG_L, B, sizeof(typename A::S), EPT>(o + r * NS, b)] = A::to_smem(a[u + r * (E / R)]);
         }
         __syncthreads();
     }
@@ -220,6 +256,63 @@ __device__ __forceinline__ void stages16(typename A::C *a, typename A::S *sm, in
     }
 }
 
+/*
+ * A radix-EPT stage after 2^lns points have been combined, with lns and
+ * whether it is the last stage known at run time: the same reads, twiddles,
+ * butterfly and writes as stage<A, LOG_L, B, EPT, 2^lns, true, !last>.
+ */
+template <class A, int LOG_L, int B, int EPT>
+__device__ __forceinline__ void stage_rt(typename A::C *a, typename A::S *sm, int j, int b,
+                                         const void *tw, int lns, bool last)
+{
+    using C = typename A::C;
+    using SH = Shape<LOG_L, EPT>;
+    constexpr int E = SH::E, TPL = SH::TPL, R = EPT, LR = SH::LE;
+    constexpr int ES = (int)sizeof(typename A::S);
+#pragma unroll
+    for (int q = 0; q < E; q++) a[q] = A::from_smem(sm[sidx<LOG_L, B, ES, EPT>(j + q * TPL, b)]);
+    const int ns = 1 << lns;
+#pragma unroll
+    for (int u = 0; u < E / R; u++) {
+        C c[R];
+#pragma unroll
+        for (int r = 0; r < R; r++) c[r] = a[u + r * (E / R)];
+        const int k = (j + u * TPL) & (ns - 1);
+        const int sh = LOG_L - lns - LR; /* W_{ns R}^{r k} = W_L^{r k L / (ns R)} */
+#pragma unroll
+        for (int r = 1; r < R; r++) c[r] = A::mul_tw(c[r], A::load_tw(tw, (int64_t)(r * k) << sh));
+        dft<A, R>(c);
+#pragma unroll
+        for (int r = 0; r < R; r++) a[u + r * (E / R)] = c[r];
+    }
+    if (!last) { /* CTA-uniform */
+        __syncthreads();
+#pragma unroll
+        for (int u = 0; u < E / R; u++) {
+            const int jj = j + u * TPL;
+            const int k = jj & (ns - 1);
+            const int o = ((jj >> lns) << (lns + LR)) + k;
+#pragma unroll
+            for (int r = 0; r < R; r++)
+                sm[sidx<LOG_L, B, ES, EPT>(o + r * ns, b)] = A::to_smem(a[u + r * (E / R)]);
+        }
+        __syncthreads();
+    }
+}
+
+/* Double-float butterflies are long (a radix-16 stage is over a thousand
+ * instructions per thread).  The FP64-storage kernel's lines of three or
+ * more stages run the stages after the first as one loop with the stage
+ * index at run time: one copy of the butterfly instead of one per stage,
+ * which keeps the kernel's code within the instruction cache (measured 5.6%
+ * faster at 2^24; the FP32-storage double-float kernel measured 0.9% slower
+ * rolled at 512^3 and keeps its stages unrolled). */
+template <class A, int LOG_L, int EPT>
+__host__ __device__ constexpr bool roll_stages()
+{
+    return A::kId == 1 && Shape<LOG_L, EPT>::NSTAGE >= 3;
+}
+
 template <class A, int LOG_L, int B, int EPT = 16>
 __device__ __forceinline__ void fft_line_regs(typename A::C *a, typename A::S *sm, int j, int b,
                                               const void *tw)
@@ -232,7 +325,14 @@ __device__ __forceinline__ void fft_line_regs(typename A::C *a, typename A::S *s
     } else {
         constexpr int R_first = SH::LR0 ? SH::R0 : EPT;
         stage<A, LOG_L, B, R_first, 1, false, true, EPT>(a, sm, j, b, tw);
-        stages16<A, LOG_L, B, 1, EPT>(a, sm, j, b, tw);
+        if constexpr (roll_stages<A, LOG_L, EPT>()) {
+            constexpr int first_log = SH::LR0 ? SH::LR0 : SH::LE;
+#pragma unroll 1
+            for (int s = 1; s < SH::NSTAGE; s++)
+                stage_rt<A, LOG_L, B, EPT>(a, sm, j, b, tw, first_log + SH::LE * (s - 1), s == SH::NSTAGE - 1);
+        } else {
+            stages16<A, LOG_L, B, 1, EPT>(a, sm, j, b, tw);
+        }
     }
 }
 
@@ -406,12 +506,21 @@ __device__ __forceinline__ bool mbar_wait0(uint32_t mbar)
  * A full tile of B contiguous lines (ies == 1, is[0] == L) staged through
  * shared memory: an mbarrier after the exchange buffer, one bulk
  * asynchronous copy per line (issued by threads 0..B-1, evict-first in L2)
- * into a slot of L elements plus 32 bytes (the padding spreads the lines'
- * first elements over the banks), then each thread reads its E points from
- * its line's slot.
+ * into a slot of L elements plus 16 bytes, then each thread reads its E
+ * points from its line's slot.  The 16-byte pad (the least a bulk copy's
+ * destination alignment allows) makes the slot stride an odd number of
+ * 16-byte units: the B lines' elements of one phase of a warp's read (8
+ * lines of 16-byte or 2 x 8 lines of 8-byte elements) then fall in distinct
+ * banks; a 32-byte pad put lines b and b + 4 on the same banks.
  * Ends with a barrier: the stages reuse the buffer.  A wait that gives up
  * sets *p.err and waits once more (bounded) for the copies in flight.
  */
+/* bytes per line slot of bulk_load_tile: the line plus a 16-byte pad */
+__host__ __device__ constexpr size_t bulk_slot_bytes(int log_l, int store_bytes)
+{
+    return ((size_t)1 << log_l) * (size_t)store_bytes + 16;
+}
+
 template <class A, int LOG_L, int B, int E, int TPL>
 __device__ __forceinline__ void bulk_load_tile(const tfft_pass &p, const TileGeom &g,
                                                typename A::Store (&raw)[E], unsigned char *smem_raw,
@@ -421,7 +530,7 @@ __device__ __forceinline__ void bulk_load_tile(const tfft_pass &p, const TileGeo
     using Store = typename A::Store;
     constexpr int L = 1 << LOG_L;
     constexpr uint32_t LINE_BYTES = (uint32_t)(L * sizeof(Store));
-    constexpr size_t SLOT = (size_t)LINE_BYTES + 32;
+    constexpr size_t SLOT = bulk_slot_bytes(LOG_L, (int)sizeof(Store));
     static_assert(B * SLOT <= pass_smem_bytes<A, LOG_L, B>(), "staging slots inside the exchange buffer");
     const uint32_t mbar = smem_addr32(smem_raw + pass_smem_bytes<A, LOG_L, B>());
     const int t = threadIdx.x;
@@ -587,15 +696,18 @@ __device__ __forceinline__ void run_tile(const tfft_pass &p, int64_t tile, unsig
 }
 
 /* Minimum CTAs per SM in the launch bounds.  0 leaves the register count to
- * ptxas's default heuristic (128 for the double-float FP32 kernel, 80 for
- * FP32); an explicit 1 lets it take up to 255 (225 and 161 registers: one CTA
- * per SM, measured 20-35% slower).  The double-float FP64-storage kernel
- * asks for 16 resident warps (16/W CTAs of W warps, at most 128 registers). */
+ * ptxas's default heuristic (128 for the double-float FP32 kernel); an
+ * explicit 1 lets it take up to 255 (225 and 161 registers: one CTA per SM,
+ * measured 20-35% slower).  The double-float FP64-storage kernel asks for
+ * 16 resident warps (16/W CTAs of W warps, at most 128 registers).  The FP32
+ * kernel's 256-thread CTAs ask for three per SM (at most 85 registers):
+ * left alone, the staged-tile path took it to 92 registers and two CTAs,
+ * 7.5% slower on 512^3 despite the few spills the cap costs. */
 template <class A, int T>
 constexpr int pass_min_blocks()
 {
     constexpr int W = (T + 31) / 32;
-    return A::kScaled && W < 16 ? 16 / W : 0;
+    return A::kScaled && W < 16 ? 16 / W : (A::kId == 2 && W == 8) ? 3 : 0;
 }
 
 template <class A, int LOG_L, int B, int EPT = 16>

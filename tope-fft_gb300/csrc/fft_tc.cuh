@@ -223,7 +223,7 @@ __device__ __forceinline__ void stage16(ArithDF32::C *a, float4 *sm, int j, int 
     if (cx.dead) return; /* CTA-uniform */
     if constexpr (FROM_SMEM) {
 #pragma unroll
-        for (int q = 0; q < 16; q++) a[q] = A::from_smem(sm[sidx<B>(j + q * TPL, b)]);
+        for (int q = 0; q < 16; q++) a[q] = A::from_smem(sm[sidx<LOG_L, B, sizeof(float4)>(j + q * TPL, b)]);
     }
     if constexpr (RENORM) {
 #pragma unroll
@@ -301,7 +301,7 @@ __device__ __forceinline__ void stage16(ArithDF32::C *a, float4 *sm, int j, int 
         const int k = j & (NS - 1);
         const int o = (j / NS) * NS * 16 + k;
 #pragma unroll
-        for (int r = 0; r < 16; r++) sm[sidx<B>(o + r * NS, b)] = A::to_smem(a[r]);
+        for (int r = 0; r < 16; r++) sm[sidx<LOG_L, B, sizeof(float4)>(o + r * NS, b)] = A::to_smem(a[r]);
     }
     /* the exchange barrier, which also makes a give-up CTA-uniform */
     if (__syncthreads_or(!ok)) {
