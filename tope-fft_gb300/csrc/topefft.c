@@ -323,14 +323,18 @@ static int pow2_divisor(int64_t v, int cap)
 }
 
 /* lines per CTA: about 256 threads, at least 8 adjacent lines when the
- * line itself is strided (128-byte segments), at most 8192 points per CTA */
-static int choose_b(int log_l, int64_t n0, int strided, int ept)
+ * line itself is strided (128-byte segments), at most 8192 points per CTA.
+ * Strided native-FP64 lines of 4096 points are the exception (f64): their
+ * pass is bound by the FP64 pipe, and one line per CTA (256-thread CTAs, two
+ * per SM) measured 4.8% faster at 2^24 than two lines per 512-thread CTA;
+ * the double-float and FP32-storage passes measured up to 12% slower so. */
+static int choose_b(int log_l, int64_t n0, int strided, int ept, int f64)
 {
     int64_t L = (int64_t)1 << log_l;
     int64_t e = L < ept ? L : ept;
     int64_t want = 256 * e / L;
     if (want < 1) want = 1;
-    if (strided && want < 8) want = 8;
+    if (strided && want < 8 && !(f64 && L >= 4096)) want = 8;
     int64_t maxb = (ept == 4 ? 4096 : 8192) / L;
     if (maxb > 32) maxb = 32;
     if (want > maxb) want = maxb;
@@ -500,7 +504,8 @@ static int add_pass(struct topeFFT *f, tope_impl *P, int64_t len, int64_t ies, i
                  : 0;
     int b = (nl == 0) ? 1
             : mixed   ? choose_b_mixed(len, p->n[0])
-                      : choose_b(log_l, p->n[0], strided, p->ept ? 4 : 16);
+                      : choose_b(log_l, p->n[0], strided, p->ept ? 4 : 16,
+                                 P->arith == TFFT_ARITH_F64);
     /* few lines (small single transforms): spread them over at least 32 CTAs
      * rather than keep wide tiles */
     while (b > 1 && p->n[0] * p->n[1] * p->n[2] / b < 32) b >>= 1;
