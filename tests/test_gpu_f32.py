@@ -95,10 +95,11 @@ def test_f32_error_vs_fp64_oracle(T, fw, orc, dims, batch):
         assert err <= fw.gate and err_alg <= fw.gate
 
 
-@pytest.mark.parametrize("dims,batch", [((512, 512, 512), 1), ((1 << 14, 1, 1), 4096)],
-                         ids=["512^3", "4096x2^14"])
+@pytest.mark.parametrize("dims,batch", [((512, 512, 512), 1), ((1 << 14, 1, 1), 4096), ((1 << 24, 1, 1), 1)],
+                         ids=["512^3", "4096x2^14", "2^24"])
 def test_f32_full_size(T, fw, orc, dims, batch):
-    """The split-precision benchmark configurations themselves."""
+    """The split-precision benchmark configurations themselves, and the 2^24
+    line of the default benchmark's split-precision companion."""
     x = pulse_field(orc, dims, batch)
     x32 = x.astype(np.float32)
     got = run_f32(T, fw, x32, dims, 1, batch).astype(np.float64)

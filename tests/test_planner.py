@@ -167,9 +167,17 @@ def test_real_plans_transform_half_length_rows(T, S, fw):
 
 def test_split_precision_shapes(T, S, fw):
     """FP32 storage takes 2^14-point lines in one pass, so 2^29 points are three
-    passes; the tensor form uses its fixed tiles and rejects mixed radix."""
+    passes; 2^24..2^26 points take three short passes too (2^23, as a real
+    plan's line, keeps two); the tensor form uses its fixed tiles and rejects
+    mixed radix."""
     p = passes(S, fw, plan1d(T, S, fw, 1 << 29, f32=True))
     assert [q["len"] for q in p] == [1024, 1024, 512]
+    p = passes(S, fw, plan1d(T, S, fw, 1 << 24, f32=True))
+    assert [q["len"] for q in p] == [256, 256, 256]
+    p = passes(S, fw, plan1d(T, S, fw, 1 << 23, f32=True))
+    assert [q["len"] for q in p] == [4096, 2048]
+    p = passes(S, fw, plan1d(T, S, fw, 1 << 24))
+    assert [q["len"] for q in p] == [4096, 4096]
     S.topeSetSplitMode(C.byref(fw), 2)
     p = passes(S, fw, plan1d(T, S, fw, 1 << 20, f32=True))
     assert [(q["len"], q["b"]) for q in p] == [(1024, 4), (1024, 4)]

@@ -792,6 +792,16 @@ static int plan_axis(struct topeFFT *f, tope_impl *P, int axis)
             /* four-step: two passes up to 2^(2*max_lg) points, one more per
              * further factor of 2^max_lg */
             parts = lg <= 2 * max_lg ? 2 : (lg + max_lg - 1) / max_lg;
+            /* FP32 storage moves half the bytes per pass, and its 2^12-point
+             * passes cost more per bit than short ones (three radix-16 stages
+             * in one CTA of two strided lines): 2^24..2^26-point lines take
+             * three passes of 2^8..2^9 points.  Measured at 2^24: accurate
+             * 1.24 -> 1.12 ms per step, fast 0.82 -> 0.62, tensor 1.62 ->
+             * 1.26; a real plan's 2^23-point line was 7% slower so, and keeps
+             * two passes. */
+            if (parts == 2 && lg >= 24 &&
+                (P->arith == TFFT_ARITH_DF32 || P->arith == TFFT_ARITH_F32 || P->arith == TFFT_ARITH_TC))
+                parts = 3;
         } else {
             parts = 2;
             while (parts <= 6 && !fits_parts(P, n, parts)) parts++;
