@@ -452,14 +452,23 @@ static int merge_dims(dimref *d, int n)
 }
 
 /* How plans load full tiles (the same transform, other load paths: for
- * comparing them).  TOPEFFT_BULK=0: every tile directly; 1 (the default):
- * tiles of contiguous lines by bulk copies, strided ones directly; 2: strided
- * tiles by TMA boxes from tensor maps as well (measured 1.5-4% slower than
- * direct loads on the FP32 and double-float 3D shapes) */
+ * comparing them).  TOPEFFT_BULK=0: every tile directly; 1: tiles of
+ * contiguous lines by bulk copies, strided ones directly; 2: strided tiles by
+ * TMA boxes from tensor maps as well.  Unset (-1): contiguous tiles by bulk
+ * copies, and strided tiles by TMA boxes in the double-float FP64-storage
+ * arithmetic only, the one where they measured faster (256^3: 1.3%; FP32
+ * storage and native FP64 were 0-4% slower so). */
 static int bulk_level(void)
 {
     const char *e = getenv("TOPEFFT_BULK");
-    return !e || !e[0] ? 1 : e[0] == '0' ? 0 : e[0] == '2' ? 2 : 1;
+    return !e || !e[0] ? -1 : e[0] == '0' ? 0 : e[0] == '2' ? 2 : 1;
+}
+
+/* stage full tiles of adjacent strided lines by TMA in this arithmetic? */
+static int tma_enabled(int arith)
+{
+    const int lv = bulk_level();
+    return lv == 2 || (lv < 0 && arith == TFFT_ARITH_DF64);
 }
 
 /* one pass over lines of len points (a power of two, or a smooth length for
@@ -519,7 +528,7 @@ static int add_pass(struct topeFFT *f, tope_impl *P, int64_t len, int64_t ies, i
      * bulk asynchronous copies; a wait for them that gives up sets the plan's
      * device word, which the synchronous Exec reports */
     if (!mixed && nl > 0 && ies == 1 && p->is[0] == ((int64_t)1 << log_l) && !p->tab0 &&
-        bulk_level() >= 1 && tfft_pass_bulk_capable(log_l, b, P->arith, p->ept)) {
+        bulk_level() != 0 && tfft_pass_bulk_capable(log_l, b, P->arith, p->ept)) {
         if (!P->err_word) {
             void *w;
             int st = impl_alloc_tab(P, 16, -1, &w);
@@ -530,7 +539,7 @@ static int add_pass(struct topeFFT *f, tope_impl *P, int64_t len, int64_t ies, i
         }
         p->bulk = 1;
         p->err = P->err_word;
-    } else if (!mixed && nl > 0 && ies != 1 && p->is[0] == 1 && !p->tab0 && bulk_level() >= 2 &&
+    } else if (!mixed && nl > 0 && ies != 1 && p->is[0] == 1 && !p->tab0 && tma_enabled(P->arith) &&
                tfft_pass_bulk_capable(log_l, b, P->arith, p->ept)) {
         /* adjacent strided lines: TMA boxes from a tensor map, built once
          * the plan's buffers exist (plan_tensor_maps) */
