@@ -17,8 +17,11 @@
 static uintptr_t g_next = 0x100000;
 
 /* call log for the tests: kind 1 = pass launch {n0, n1, n2, in, out, len or
- * -log2 L, flags: 1 conj_in, 2 conj_out, 4 scaled}, kind 2 = device-to-host copy {dst, src, bytes}, kind 3 = 2D
- * device-to-host copy {dst, src, width, height, pitch} */
+ * -log2 L, flags: 1 conj_in, 2 conj_out, 4 scaled, 8 tensor map, 16 bulk
+ * copies}, kind 2 = device-to-host copy {dst, src, bytes}, kind 3 = 2D
+ * device-to-host copy {dst, src, width, height, pitch}, kind 4 = tensor map
+ * {rank, dims[0..3], box[0], box[1]} followed by kind 5 {strides[0..2],
+ * box[2], box[3], base} */
 #define LOG_MAX 4096
 static int64_t g_log[LOG_MAX][8];
 static int g_nlog = 0;
@@ -111,7 +114,8 @@ int tfft_launch_pass(const tfft_pass *p, void *s)
     (void)s;
     log_rec(1, p->n[0], p->n[1], p->n[2], (int64_t)(uintptr_t)p->in, (int64_t)(uintptr_t)p->out,
             p->len ? p->len : -(int64_t)p->log_l,
-            (p->conj_in ? 1 : 0) | (p->conj_out ? 2 : 0) | (p->scale != 1.0 ? 4 : 0));
+            (p->conj_in ? 1 : 0) | (p->conj_out ? 2 : 0) | (p->scale != 1.0 ? 4 : 0) |
+                (p->tmap ? 8 : 0) | (p->bulk ? 16 : 0));
     return 0;
 }
 
@@ -135,20 +139,35 @@ int tfft_pass_supported(int log_l, int b_tile, int arith, int ept)
     return (log_l + lb) <= (arith == TFFT_ARITH_F32 ? 14 : 13);
 }
 
-/* no stand-in kernel stages tiles with bulk copies: the planner's copy and
- * launch logs stay those of direct loads */
+/* Staged tiles: off by default (no stand-in kernel stages tiles, and every
+ * tensor map fails, so the plans load directly); stub_set_staging(1) answers
+ * as the real library does (fft_dispatch.cu, fft_tma.cu), logging each map */
+static int g_staging = 0;
+void stub_set_staging(int on) { g_staging = on; }
+
 int tfft_pass_bulk_capable(int log_l, int b_tile, int arith, int ept)
 {
-    (void)log_l; (void)b_tile; (void)arith; (void)ept;
-    return 0;
+    if (!g_staging) return 0;
+    if (arith == TFFT_ARITH_TC || (ept != 0 && ept != 16)) return 0;
+    if (b_tile < 8 || log_l < 5 || ((int64_t)TFFT_ELEM_BYTES(arith) << log_l) < 512) return 0;
+    return tfft_pass_supported(log_l, b_tile, arith, ept);
 }
 
-/* no tensor maps in the stand-in: strided passes load directly */
 int tfft_tensor_map(void *dev_map, const void *base, int rank, const int64_t *dims,
                     const int64_t *strides, const int *box)
 {
-    (void)dev_map; (void)base; (void)rank; (void)dims; (void)strides; (void)box;
-    return 1;
+    (void)dev_map;
+    if (!g_staging) return 1;
+    if (rank < 2 || rank > 4) return 1;
+    int64_t d[4] = {0, 0, 0, 0}, st[3] = {0, 0, 0}, bx[4] = {0, 0, 0, 0};
+    for (int k = 0; k < rank; k++) {
+        d[k] = dims[k];
+        bx[k] = box[k];
+        if (k > 0) st[k - 1] = strides[k - 1];
+    }
+    log_rec(4, rank, d[0], d[1], d[2], d[3], bx[0], bx[1]);
+    log_rec(5, st[0], st[1], st[2], bx[2], bx[3], (int64_t)(uintptr_t)base, 0);
+    return 0;
 }
 
 int tfft_mixed_supported(int len, int b_tile, int arith)

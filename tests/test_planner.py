@@ -364,3 +364,76 @@ def test_largest_plans(T, S, fw, f32, real, dims, batch, status):
         assert fw.error == T.TOPE_SUCCESS
     destroy(C.byref(fw), C.byref(t))
     assert fw.error == T.TOPE_SUCCESS and not t.impl
+
+
+# ---------------------------------------------------------------- staged tiles
+def staging_log(T, S, fw, monkeypatch, arith, level):
+    """Plan 256^3 in `arith` with TOPEFFT_BULK=`level` (None: unset) and the
+    stub answering as the real library, run it on the device (no read-back
+    slicing) and return (tensor maps as (rank, dims, strides, box), launch
+    flags per pass)."""
+    if level is None:
+        monkeypatch.delenv("TOPEFFT_BULK", raising=False)
+    else:
+        monkeypatch.setenv("TOPEFFT_BULK", level)
+    S.topeSetArith(C.byref(fw), arith)
+    S.stub_set_staging(1)
+    try:
+        S.stub_log_clear()
+        t = T.TopePlan3D()
+        S.tope3DPlanInit(C.byref(fw), C.byref(t), 256, 256, 256, T.C2C, None)
+        assert fw.error == T.TOPE_SUCCESS
+        recs = call_log(S)
+        maps = []
+        for a, b in zip(recs, recs[1:]):
+            if a[0] == 4:
+                rank = a[1]
+                maps.append((rank, a[2:2 + rank], b[1:rank], [a[6], a[7], b[4], b[5]][:rank]))
+        S.stub_log_clear()
+        S.tope3DExecDevice(C.byref(fw), C.byref(t), T.FORWARD)
+        assert fw.error == T.TOPE_SUCCESS
+        flags = [r[7] & 24 for r in call_log(S) if r[0] == 1]
+        S.tope3DDestroy(C.byref(fw), C.byref(t))
+        return maps, flags
+    finally:
+        S.stub_set_staging(0)
+
+
+def test_staged_tiles_and_tensor_maps(T, S, fw, monkeypatch):
+    """256^3: the x pass (contiguous lines, 16 per CTA) stages its tiles by
+    bulk copies; the y and z passes (adjacent strided lines) by TMA boxes
+    from tensor maps in 8-byte units, dimension 0 the adjacent lines, then the
+    line and the other line dimensions by stride, box 16 lines x 256 points.
+    By default only the double-float FP64 arithmetic takes the maps;
+    TOPEFFT_BULK=2 gives them to native FP64 too, 1 keeps the bulk copies
+    only, 0 loads every tile directly."""
+    y_map = (3, [512, 256, 256], [16 * 256, 16 * 65536], [32, 256, 1])
+    z_map = (2, [2 * 65536, 256], [16 * 65536], [32, 256])
+    maps, flags = staging_log(T, S, fw, monkeypatch, T.TOPE_ARITH_DF64, None)
+    assert maps == [y_map, z_map] and flags == [16, 8, 8]
+    maps, flags = staging_log(T, S, fw, monkeypatch, T.TOPE_ARITH_FP64, None)
+    assert maps == [] and flags == [16, 0, 0]
+    maps, flags = staging_log(T, S, fw, monkeypatch, T.TOPE_ARITH_FP64, "2")
+    assert maps == [y_map, z_map] and flags == [16, 8, 8]
+    maps, flags = staging_log(T, S, fw, monkeypatch, T.TOPE_ARITH_DF64, "1")
+    assert maps == [] and flags == [16, 0, 0]
+    maps, flags = staging_log(T, S, fw, monkeypatch, T.TOPE_ARITH_DF64, "0")
+    assert maps == [] and flags == [0, 0, 0]
+
+
+def test_readback_slices_drop_the_tensor_map(T, S, fw, monkeypatch):
+    """A read-back slice of the last pass covers part of the array, which the
+    pass's tensor map does not describe: its launches load directly."""
+    monkeypatch.delenv("TOPEFFT_BULK", raising=False)
+    S.topeSetArith(C.byref(fw), T.TOPE_ARITH_DF64)
+    S.stub_set_staging(1)
+    try:
+        t = T.TopePlan3D()
+        S.tope3DPlanInit(C.byref(fw), C.byref(t), 256, 256, 256, T.C2C, None)
+        log, _ = exec_log(T, S, fw, t, S.tope3DExec, np.zeros(2))
+        launches = [r for r in log if r[0] == 1]
+        assert len(launches) == 2 + 8
+        assert launches[1][7] & 8 and not any(r[7] & 8 for r in launches[2:])
+        S.tope3DDestroy(C.byref(fw), C.byref(t))
+    finally:
+        S.stub_set_staging(0)
