@@ -225,6 +225,13 @@ __device__ __forceinline__ void stage16(ArithDF32::C *a, float4 *sm, int j, int 
 #pragma unroll
         for (int q = 0; q < 16; q++) a[q] = A::from_smem(sm[sidx<LOG_L, B, sizeof(float4)>(j + q * TPL, b)]);
     }
+    if constexpr (FROM_SMEM && TO_SMEM) {
+        /* every thread's reads of the exchange buffer before any thread's
+         * writes at the end of this stage: a line spans both row groups,
+         * which otherwise meet only at their own named barriers until the
+         * stage's closing barrier */
+        __syncthreads();
+    }
     if constexpr (RENORM) {
 #pragma unroll
         for (int q = 0; q < 16; q++) {
