@@ -16,19 +16,19 @@
 
 #include "tfft_abi.h"
 
+/* the driver's encoder, looked up once (a function-local static: its
+ * initialisation is thread-safe when plans are made from several threads) */
 static PFN_cuTensorMapEncodeTiled_v12000 encode_fn(void)
 {
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-    static int tried = 0;
-    if (!tried) {
-        tried = 1;
+    static const PFN_cuTensorMapEncodeTiled_v12000 fn = []() -> PFN_cuTensorMapEncodeTiled_v12000 {
         void *p = nullptr;
         cudaDriverEntryPointQueryResult q;
         if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
                                              &q) == cudaSuccess &&
             q == cudaDriverEntryPointSuccess)
-            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-    }
+            return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+        return nullptr;
+    }();
     return fn;
 }
 
