@@ -4,7 +4,9 @@ built through the public entry points and their pass structure is read back
 with topePassInfo, with no GPU.  Covers the decisions the GPU tests rely on:
 one pass or a four-step split, three-pass lines, the small-transform shape,
 mixed-radix splits, the Bluestein sub-transform size, real-data row plans and
-the tensor form's tiles, and plans of up to 2^33 points in every form.
+the tensor form's tiles, plans of up to 2^33 points in every form, staged
+tiles and tensor maps, and (with hypothesis) random power-of-two and smooth
+plans whose passes must cover every axis.
 
 The host code is built with UndefinedBehaviorSanitizer where the compiler has
 its runtime: a signed overflow, an out-of-range shift or a misaligned access in
@@ -437,3 +439,88 @@ def test_readback_slices_drop_the_tensor_map(T, S, fw, monkeypatch):
         S.tope3DDestroy(C.byref(fw), C.byref(t))
     finally:
         S.stub_set_staging(0)
+
+
+# ---------------------------------------------------------------- properties
+hyp = pytest.importorskip("hypothesis")
+st = pytest.importorskip("hypothesis.strategies")
+
+
+@hyp.settings(max_examples=200, deadline=None,
+              suppress_health_check=[hyp.HealthCheck.function_scoped_fixture])
+@hyp.given(dims=st.lists(st.integers(0, 13), min_size=1, max_size=3),
+           lg1d=st.integers(1, 30), batch_lg=st.integers(0, 6),
+           form=st.sampled_from(["fp64", "df64", "accurate", "fast", "tensor"]))
+def test_power_of_two_plans_cover_every_axis(T, S, fw, dims, lg1d, batch_lg, form):
+    """Any power-of-two plan within the limits: every pass is a shape the
+    kernels have, runs at most 1024 threads per CTA, and the pass lengths
+    multiply to the transform's size (each axis split into passes whose
+    lengths multiply to its own length); FP32-storage lines of 2^24..2^26
+    points take three passes, FP64-storage ones two."""
+    f32 = form in ("accurate", "fast", "tensor")
+    S.topeSetArith(C.byref(fw), T.TOPE_ARITH_DF64 if form == "df64" else T.TOPE_ARITH_FP64)
+    S.topeSetSplitMode(C.byref(fw), {"accurate": 0, "fast": 1, "tensor": 2}.get(form, 0))
+    if len(dims) == 1:
+        n, batch = 1 << lg1d, 1 << batch_lg
+        if n * batch > 1 << 30:
+            return
+        t = plan1d(T, S, fw, n, batch=batch, f32=f32)
+        total = n
+        destroy = S.tope1DDestroy
+    else:
+        sides = [1 << (d + 1) for d in dims] + [1] * (3 - len(dims))
+        total = sides[0] * sides[1] * sides[2]
+        if total > 1 << 30:
+            return
+        if len(dims) == 2:
+            t = T.TopePlan2D()
+            (S.tope2DPlanInitF32 if f32 else S.tope2DPlanInit)(
+                C.byref(fw), C.byref(t), sides[0], sides[1], T.C2C, None)
+            destroy = S.tope2DDestroy
+        else:
+            t = T.TopePlan3D()
+            (S.tope3DPlanInitF32 if f32 else S.tope3DPlanInit)(
+                C.byref(fw), C.byref(t), sides[0], sides[1], sides[2], T.C2C, None)
+            destroy = S.tope3DDestroy
+    assert fw.error == T.TOPE_SUCCESS, (dims, lg1d, batch_lg, form)
+    p = passes(S, fw, t)
+    if len(dims) == 1 and lg1d == 1 and batch_lg == 0 and not f32:
+        # a lone 2-point line is the reference's own N == 2 kernel (fft1d.c:16-28)
+        assert p == []
+        destroy(C.byref(fw), C.byref(t))
+        return
+    prod = 1
+    for q in p:
+        assert q["threads"] <= 1024 and q["ctas"] >= 1
+        prod *= q["len"]
+    assert prod == total
+    if len(dims) == 1 and 24 <= lg1d <= 26:
+        assert len(p) == (3 if f32 else 2)
+    destroy(C.byref(fw), C.byref(t))
+    assert fw.error == T.TOPE_SUCCESS
+
+
+@hyp.settings(max_examples=200, deadline=None,
+              suppress_health_check=[hyp.HealthCheck.function_scoped_fixture])
+@hyp.given(a=st.integers(0, 12), b=st.integers(0, 8), c=st.integers(0, 6), d=st.integers(0, 4),
+           e=st.integers(0, 2), g=st.integers(0, 2),
+           form=st.sampled_from(["fp64", "df64", "accurate", "fast"]))
+def test_smooth_lengths_split_into_their_factors(T, S, fw, a, b, c, d, e, g, form):
+    """1D lengths 2^a 3^b 5^c 7^d 11^e 13^f up to 2^30 points: the plan
+    succeeds and its passes' lengths multiply to n (mixed-radix passes for the
+    odd factors, power-of-two passes otherwise)."""
+    n = 2 ** a * 3 ** b * 5 ** c * 7 ** d * 11 ** e * 13 ** g
+    if n < 3 or n > 1 << 30:
+        return
+    f32 = form in ("accurate", "fast")
+    S.topeSetArith(C.byref(fw), T.TOPE_ARITH_DF64 if form == "df64" else T.TOPE_ARITH_FP64)
+    S.topeSetSplitMode(C.byref(fw), {"accurate": 0, "fast": 1}.get(form, 0))
+    t = plan1d(T, S, fw, n, f32=f32)
+    assert fw.error == T.TOPE_SUCCESS, (n, form)
+    p = passes(S, fw, t)
+    prod = 1
+    for q in p:
+        assert q["threads"] <= 1024 and q["ctas"] >= 1
+        prod *= q["len"]
+    assert prod == n, (n, form, [q["len"] for q in p])
+    S.tope1DDestroy(C.byref(fw), C.byref(t))
